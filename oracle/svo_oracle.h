@@ -1,0 +1,115 @@
+/*
+ * svo_oracle.h -- C interface of the CPU oracle.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is a plain CPU restatement of the
+ * reference crate shocovox-rs v0.11.1 (octree construction, update and the
+ * CPU ray cast `Octree::get_by_ray`).  It exists to check the GB300 product
+ * library (libsvo) and to time the CPU baseline.  Only the test suite,
+ * `__graft_entry__.smoke()` and the `cpu_baseline` / `--impl reference`
+ * legs of bench.py load it.  Nothing in the product links against it.
+ *
+ * Parity anchor: the reference is Rust and cannot be compiled in this
+ * environment (no cargo/rustc), so the restatement is pinned by the
+ * reference's own known-answer tests (src/raytracing/tests.rs,
+ * src/spatial/raytracing/tests.rs, src/spatial/math/tests.rs, src/octree/update/tests.rs)
+ * and by the look-up
+ * tables extracted from src/spatial/lut.rs (tests/golden/).
+ */
+#ifndef SVO_ORACLE_H
+#define SVO_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes; 1..4 mirror OctreeError (src/octree/types.rs:8-21). */
+enum {
+  ORC_OK = 0,
+  ORC_ERR_INVALID_SIZE = 1,
+  ORC_ERR_INVALID_BRICK_DIM = 2,
+  ORC_ERR_INVALID_STRUCTURE = 3,
+  ORC_ERR_INVALID_POSITION = 4,
+  ORC_ERR_REFERENCE_PANIC = 5, /* the reference would panic / overflow its stack here */
+  ORC_ERR_ARGUMENT = 6
+};
+
+/* One scene-construction operation; identical layout to svo_op in include/svo.h. */
+typedef struct {
+  uint16_t x, y, z;
+  uint8_t op;   /* 0 insert, 1 update, 2 insert_at_lod, 3 clear, 4 clear_at_lod */
+  uint8_t kind; /* bit0: albedo present, bit1: user data present */
+  uint32_t size;
+  uint32_t rgba; /* Albedo packed as Albedo::from(u32): 0xRRGGBBAA */
+  uint32_t user;
+} orc_op;
+
+/* Per-ray outputs of orc_cast (struct of arrays; any pointer may be NULL). */
+typedef struct {
+  uint8_t* status;       /* 0 miss, 1 hit, 2 work cap exceeded, 3 reference would panic */
+  uint8_t* brick_octant; /* octant of the hit brick inside a Leaf, 0 for UniformLeaf */
+  uint8_t* entry_kind;   /* 0 Empty, 1 Visual, 2 Informative, 3 Complex */
+  uint32_t* node_key;
+  uint32_t* voxel_index; /* flat index inside the brick, 0xFFFFFFFF for a Solid brick */
+  uint32_t* pix;         /* PaletteIndexValues of the hit voxel */
+  uint32_t* albedo;      /* 0xRRGGBBAA, 0 when the entry has no albedo */
+  uint32_t* user;        /* user data, 0 when the entry has none */
+  float *px, *py, *pz;   /* impact point */
+  float *nx, *ny, *nz;   /* impact normal */
+  uint32_t* node_visits; /* instrumentation: inner traversal-loop iterations */
+  uint32_t* child_reads; /* instrumentation: child-key reads */
+  uint32_t* voxel_reads; /* instrumentation: brick voxel reads */
+} orc_hits;
+
+int orc_new(uint32_t size, uint32_t brick_dim, void** out);
+void orc_free(void* tree);
+void orc_set_auto_simplify(void* tree, int enabled);
+int orc_insert(void* tree, uint32_t x, uint32_t y, uint32_t z, uint32_t kind, uint32_t rgba, uint32_t user);
+int orc_update(void* tree, uint32_t x, uint32_t y, uint32_t z, uint32_t kind, uint32_t rgba, uint32_t user);
+int orc_insert_at_lod(void* tree, uint32_t x, uint32_t y, uint32_t z, uint32_t size, uint32_t kind,
+                      uint32_t rgba, uint32_t user);
+int orc_clear(void* tree, uint32_t x, uint32_t y, uint32_t z);
+int orc_clear_at_lod(void* tree, uint32_t x, uint32_t y, uint32_t z, uint32_t size);
+int orc_apply_ops(void* tree, const orc_op* ops, uint64_t n, uint64_t* n_done);
+int orc_get(void* tree, uint32_t x, uint32_t y, uint32_t z, uint32_t out_kind_rgba_user[3]);
+
+/* Casts n rays (SoA f32 origin / direction) with `threads` host threads. */
+int orc_cast(void* tree, uint64_t n, const float* ox, const float* oy, const float* oz, const float* dx,
+             const float* dy, const float* dz, const orc_hits* out, int threads);
+
+/* Structure inspection (canonical per-node records, palettes). */
+uint64_t orc_node_count(void* tree);
+int orc_node_record(void* tree, uint64_t key, uint64_t rec[40]);
+uint64_t orc_palette(void* tree, int which, uint32_t* out, uint64_t max);
+
+/* Look-up tables generated with the reference's generator functions. */
+void orc_luts(uint64_t ray_to_node[512], uint32_t octant_step[27], uint64_t octant_mask[8],
+              uint8_t bitmap_index[64], float octant_offset[24]);
+
+/* Spatial helpers exposed for the ported spatial tests. */
+int orc_intersect_ray(const float cube[4], const float ray[6], float* distance); /* 0 none, 1 inside, 2 dist */
+void orc_cube_impact_normal(const float cube[4], const float point[3], float out[3]);
+uint32_t orc_hash_region(const float offset[3], float size_half);
+uint64_t orc_position_in_bitmap(uint64_t x, uint64_t y, uint64_t z, uint64_t brick_size);
+uint64_t orc_set_occupancy(uint64_t x, uint64_t y, uint64_t z, uint64_t size, uint64_t brick_dim, int occupied,
+                           uint64_t bitmap);
+int orc_plane_line_intersection(const float plane_point[3], const float plane_normal[3], const float line_origin[3],
+                                const float line_direction[3], float* out);
+void orc_child_bounds(const float cube[4], uint32_t octant, float out[4]);
+void orc_dda_step(const float ray[6], float point[3], const float cube[4], float step_out[3]);
+uint64_t orc_flat_projection(uint64_t x, uint64_t y, uint64_t z, uint64_t size);
+
+/* NodeStack<i32, size> harness for the ported ring-stack tests (size 1..8). */
+void* orc_stack_new(uint32_t size);
+void orc_stack_free(void* s);
+void orc_stack_push(void* s, int32_t v);
+int orc_stack_pop(void* s, int32_t* out);      /* 1 = Some, 0 = None */
+int orc_stack_last(void* s, int32_t* out);     /* 1 = Some, 0 = None */
+int orc_stack_add_last(void* s, int32_t delta); /* last_mut += delta; 1 = Some */
+int orc_stack_is_empty(void* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
