@@ -1,0 +1,210 @@
+/*
+ * svo.h -- C ABI of libsvo, the GB300-native sparse voxel octree ray caster.
+ *
+ * libsvo keeps the API surface of shocovox-rs v0.11.1 for the ray-cast hot
+ * path: octree construction and update (host side), a device-resident image
+ * of the octree that is uploaded once and then updated in place, and the
+ * first-hit ray cast `get_by_ray` run as sm_103a CUDA kernels.
+ *
+ * Conventions
+ *  - Every entry point returns an svo_status; 0 is success.  No C++
+ *    exception or panic crosses this boundary.  svo_last_error() returns a
+ *    thread-local message for the last failure on the calling thread.
+ *  - `stream` arguments are cudaStream_t values passed as void* (NULL is the
+ *    legacy default stream).  All GPU work is stream ordered; no entry point
+ *    synchronises the device except the *_host convenience calls, which
+ *    synchronise their stream before returning.
+ *  - An svo_scene is externally synchronised for construction/update (like
+ *    `&mut Octree`); casts on an uploaded scene may run concurrently on any
+ *    number of streams (like `&Octree`).
+ *  - Albedo values are packed as the reference's `Albedo::from(u32)` reads
+ *    them: 0xRRGGBBAA.  User data is the reference's default T = u32.
+ */
+#ifndef SVO_H
+#define SVO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t svo_status;
+enum {
+  SVO_OK = 0,
+  SVO_ERR_INVALID_SIZE = 1,        /* OctreeError::InvalidSize (src/octree/types.rs:11) */
+  SVO_ERR_INVALID_BRICK_DIM = 2,   /* OctreeError::InvalidBrickDimension (types.rs:14) */
+  SVO_ERR_INVALID_STRUCTURE = 3,   /* OctreeError::InvalidStructure (types.rs:17) */
+  SVO_ERR_INVALID_POSITION = 4,    /* OctreeError::InvalidPosition (types.rs:20) */
+  SVO_ERR_REFERENCE_PANIC = 5,     /* the reference panics on this input; the scene is left unusable */
+  SVO_ERR_ARGUMENT = 6,            /* NULL handle/pointer or out-of-range argument */
+  SVO_ERR_CUDA = 7,                /* a CUDA runtime call failed (see svo_last_error) */
+  SVO_ERR_NOT_UPLOADED = 8,        /* cast on a scene without a device image */
+  SVO_ERR_OUT_OF_MEMORY = 9,       /* device allocation failed */
+  SVO_ERR_BUDGET = 10,             /* a server admission exceeds its device-memory budget */
+  SVO_ERR_NOT_FOUND = 11,          /* unknown server scene / request id */
+  SVO_ERR_BUSY = 12                /* request queue full or a result not ready yet */
+};
+
+/* Per-ray status codes written by the cast. */
+enum {
+  SVO_RAY_MISS = 0,
+  SVO_RAY_HIT = 1,
+  SVO_RAY_WORK_CAP = 2,      /* 2^22 traversal steps exceeded: the reference would loop forever */
+  SVO_RAY_REFERENCE_PANIC = 3 /* the reference indexes BITMAP_INDEX_LUT out of bounds on this ray */
+};
+
+/* Operation kinds of svo_op (construction recipes shared by tests and benches). */
+enum { SVO_OP_INSERT = 0, SVO_OP_UPDATE = 1, SVO_OP_INSERT_AT_LOD = 2, SVO_OP_CLEAR = 3, SVO_OP_CLEAR_AT_LOD = 4 };
+/* Entry kinds (OctreeEntry, src/octree/types.rs:23-36): bit0 albedo, bit1 user data. */
+enum { SVO_ENTRY_EMPTY = 0, SVO_ENTRY_VISUAL = 1, SVO_ENTRY_INFORMATIVE = 2, SVO_ENTRY_COMPLEX = 3 };
+
+typedef struct svo_scene svo_scene;
+
+typedef struct {
+  uint16_t x, y, z;
+  uint8_t op;   /* SVO_OP_* */
+  uint8_t kind; /* SVO_ENTRY_* bits */
+  uint32_t size;
+  uint32_t rgba;
+  uint32_t user;
+} svo_op; /* 20 bytes */
+
+/* Rays as six f32 arrays (struct of arrays), device or host memory per call. */
+typedef struct {
+  const float *ox, *oy, *oz;
+  const float *dx, *dy, *dz;
+} svo_rays;
+
+/* Per-ray results (struct of arrays).  Any pointer may be NULL to skip that output. */
+typedef struct {
+  uint8_t* status;       /* SVO_RAY_* */
+  uint8_t* brick_octant; /* octant of the hit brick inside a Leaf node, 0 for a UniformLeaf */
+  uint8_t* entry_kind;   /* SVO_ENTRY_* of the hit voxel */
+  uint32_t* node_key;    /* key of the leaf node that holds the hit (reference node numbering) */
+  uint32_t* voxel_index; /* flat index x + y*D + z*D*D inside the brick, 0xFFFFFFFF for a Solid brick */
+  uint32_t* pix;         /* PaletteIndexValues of the hit voxel */
+  uint32_t* albedo;      /* 0xRRGGBBAA, 0 when the entry has no albedo */
+  uint32_t* user;        /* user data, 0 when the entry has none */
+  float *px, *py, *pz;   /* impact point */
+  float *nx, *ny, *nz;   /* impact normal */
+  uint32_t* node_visits; /* optional instrumentation counters */
+  uint32_t* child_reads;
+  uint32_t* voxel_reads;
+} svo_hits;
+
+typedef struct {
+  uint64_t nodes;         /* node pool length (reserved or not) */
+  uint64_t reserved_nodes;
+  uint64_t parted_bricks; /* live Parted bricks */
+  uint64_t colors, datas; /* palette sizes */
+  uint64_t device_bytes;  /* bytes of the device image (0 when not uploaded) */
+  uint32_t size, brick_dim;
+} svo_scene_stats;
+
+const char* svo_last_error(void);
+int32_t svo_version(void);
+
+/* ---- construction and update (host) ---------------------------------- */
+/* Octree::new (src/octree/mod.rs:380-412) */
+svo_status svo_scene_create(uint32_t size, uint32_t brick_dim, svo_scene** out);
+void svo_scene_destroy(svo_scene* scene);
+/* Octree::auto_simplify (src/octree/types.rs:203) */
+svo_status svo_set_auto_simplify(svo_scene* scene, int32_t enabled);
+/* Octree::insert (src/octree/update/insert.rs:47-56) */
+svo_status svo_insert(svo_scene* scene, uint32_t x, uint32_t y, uint32_t z, uint32_t kind, uint32_t rgba, uint32_t user);
+/* Octree::update (insert.rs:79-88) */
+svo_status svo_update(svo_scene* scene, uint32_t x, uint32_t y, uint32_t z, uint32_t kind, uint32_t rgba, uint32_t user);
+/* Octree::insert_at_lod (insert.rs:63-73) */
+svo_status svo_insert_at_lod(svo_scene* scene, uint32_t x, uint32_t y, uint32_t z, uint32_t insert_size, uint32_t kind,
+                             uint32_t rgba, uint32_t user);
+/* Octree::clear / clear_at_lod (src/octree/update/clear.rs:40-60) */
+svo_status svo_clear(svo_scene* scene, uint32_t x, uint32_t y, uint32_t z);
+svo_status svo_clear_at_lod(svo_scene* scene, uint32_t x, uint32_t y, uint32_t z, uint32_t clear_size);
+/* Applies a recipe of operations in order; *n_done receives how many succeeded. */
+svo_status svo_apply_ops(svo_scene* scene, const svo_op* ops, uint64_t n, uint64_t* n_done);
+/* Octree::get (src/octree/mod.rs:416-422) */
+svo_status svo_get(svo_scene* scene, uint32_t x, uint32_t y, uint32_t z, uint32_t* kind, uint32_t* rgba, uint32_t* user);
+svo_status svo_scene_stats_get(svo_scene* scene, svo_scene_stats* out);
+/* Canonical per-node record used to compare structures (key, content, children, bricks). */
+svo_status svo_node_record(svo_scene* scene, uint64_t key, uint64_t rec[40]);
+/* Copies palette `which` (0 colours, 1 user data); returns its length. */
+uint64_t svo_palette(svo_scene* scene, int32_t which, uint32_t* out, uint64_t max);
+
+/* ---- device image (replaces OctreeGPUHost / create_new_view / write_to_gpu,
+ *      src/raytracing/bevy/data.rs:111-166, 365-773) ----------------------- */
+/* Uploads the whole scene as device-resident pools (node records, bricks, voxel
+ * occupancy bits, palettes).  Allocates device memory. */
+svo_status svo_scene_upload(svo_scene* scene, void* stream);
+/* Writes the node records, bricks and palette entries changed since the last
+ * upload/sync in place (falls back to a full upload when a pool outgrew its
+ * device allocation). */
+svo_status svo_scene_sync(svo_scene* scene, void* stream);
+svo_status svo_scene_release_device(svo_scene* scene);
+
+/* ---- the hot path: Octree::get_by_ray (src/raytracing/raytracing_on_cpu.rs:316-565) ---- */
+/* n rays in device memory -> per-ray hits in device memory.  Allocates nothing. */
+svo_status svo_cast(svo_scene* scene, const svo_rays* rays, uint64_t n, const svo_hits* hits, void* stream);
+/* Same cast with host (ideally pinned) ray and hit buffers: host->device copy,
+ * cast, device->host copy, stream synchronised before return.  Uses a
+ * per-scene device workspace that grows on demand. */
+svo_status svo_cast_host(svo_scene* scene, const svo_rays* rays, uint64_t n, const svo_hits* hits, void* stream);
+
+/* ---- batched multi-scene cast (one persistent launch) ------------------ */
+typedef struct {
+  svo_scene* scene;
+  svo_rays rays; /* device pointers */
+  uint64_t n;
+  svo_hits hits; /* device pointers */
+} svo_batch_item;
+
+typedef struct {
+  uint32_t block;          /* threads per block (multiple of 32, <= 1024); 0 = default 128 */
+  uint32_t rays_per_chunk; /* rays a warp claims per work-queue grab; 0 = default 64 */
+  uint32_t blocks_per_sm;  /* persistent CTAs per SM; 0 = default from occupancy */
+  uint32_t reserved;
+} svo_launch_config;
+
+/* Casts every item's rays in one persistent kernel launch driven by a device
+ * work counter.  The per-launch item table and counter live in a workspace
+ * owned by `ws` (create it once; it grows only when the item count grows). */
+typedef struct svo_batch_workspace svo_batch_workspace;
+svo_status svo_batch_workspace_create(svo_batch_workspace** out);
+void svo_batch_workspace_destroy(svo_batch_workspace* ws);
+svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items, uint32_t n_items,
+                            const svo_launch_config* cfg, void* stream);
+
+/* ---- synthetic workloads (seeded, deterministic on x86_64 and aarch64) ---- */
+typedef struct {
+  uint32_t kind;      /* 0 heightfield+spheres, 1 terrain+caves, 2 sparse+uniform blocks, 3 noise+spheres */
+  uint32_t size, brick_dim;
+  uint64_t seed;
+  float occupancy;    /* target fraction for kinds 2 and 3 */
+  uint32_t spheres;   /* sphere count (kinds 0 and 3) */
+  uint32_t octaves;
+  float base_freq;
+  float height_lo, height_hi;
+  float cave_threshold; /* kind 1 */
+} svo_scene_recipe;
+/* Writes the scene's construction ops into `ops` (capacity max_ops); *n_ops gets
+ * the count (also when max_ops is too small, so callers can size the buffer). */
+svo_status svo_gen_scene(const svo_scene_recipe* recipe, svo_op* ops, uint64_t max_ops, uint64_t* n_ops);
+/* Pinhole camera rays (host memory), direction = normalize(fwd + u*right + v*up). */
+svo_status svo_gen_camera_rays(const float eye[3], const float target[3], float fov_deg, uint32_t width,
+                               uint32_t height, float* ox, float* oy, float* oz, float* dx, float* dy, float* dz);
+/* Rays with origins uniform on a sphere (center, radius) and uniform directions. */
+svo_status svo_gen_sphere_rays(const float center[3], float radius, uint64_t n, uint64_t seed, float* ox, float* oy,
+                               float* oz, float* dx, float* dy, float* dz);
+
+/* ---- diagnostics ------------------------------------------------------ */
+/* Evaluates the kernels' look-up-table arithmetic on the GPU and copies back
+ * RAY_TO_NODE_OCCUPANCY_BITMASK_LUT[64][8], OCTANT_STEP_RESULT_LUT[3][3][3] and
+ * BITMAP_MASK_FOR_OCTANT_LUT[8] (src/spatial/lut.rs) for comparison with the
+ * reference constants.  Allocates a few bytes of device memory. */
+svo_status svo_selftest_luts(uint64_t* ray_to_node, uint32_t* octant_step, uint64_t* octant_masks);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SVO_H */

@@ -1,0 +1,226 @@
+"""shocovox_gb300 -- GB300-native sparse voxel octree ray caster.
+
+Python mirror of the reference crate's API for the ray-cast path
+(shocovox-rs v0.11.1): ``Octree(size, brick_dim)`` with ``insert``,
+``insert_at_lod``, ``update``, ``clear``, ``clear_at_lod`` and ``get``
+(src/octree/**), and ``get_by_ray`` (src/raytracing/raytracing_on_cpu.rs:316)
+plus batched casts.  All work runs in libsvo (C++ host code and sm_103a CUDA
+kernels behind the C ABI in include/svo.h); this module only marshals
+arguments.  There is no CPU fallback: without libsvo nothing here works.
+"""
+import ctypes
+
+import numpy as np
+
+from ._lib import (HIT_FIELDS, OP_DTYPE, Hits, LaunchConfig, Rays, SceneRecipe, check, lib)
+
+__all__ = ["Octree", "OctreeError", "OP_DTYPE", "HIT_FIELDS", "gen_scene", "gen_camera_rays", "gen_sphere_rays",
+           "SceneRecipe", "LaunchConfig", "BatchWorkspace", "lib"]
+
+OK, INVALID_SIZE, INVALID_BRICK_DIM, INVALID_STRUCTURE, INVALID_POSITION = 0, 1, 2, 3, 4
+
+
+class OctreeError(RuntimeError):
+    """An svo_status other than SVO_OK; `.code` carries it (1..4 mirror OctreeError)."""
+
+    def __init__(self, code, msg):
+        super().__init__("%s (svo_status %d)" % (msg, code))
+        self.code = code
+
+
+def _vp(x):
+    return ctypes.c_void_p(x) if isinstance(x, int) else x
+
+
+def _np_ptr(a):
+    return a.ctypes.data if a is not None else 0
+
+
+def _entry(albedo, user):
+    kind = (1 if albedo is not None else 0) | (2 if user is not None else 0)
+    return kind, (albedo or 0) & 0xFFFFFFFF, (user or 0) & 0xFFFFFFFF
+
+
+class Octree:
+    """A scene: host octree plus (after ``upload``) its device-resident image."""
+
+    def __init__(self, size, brick_dim):
+        h = ctypes.c_void_p()
+        rc = lib().svo_scene_create(size, brick_dim, ctypes.byref(h))
+        if rc != 0:
+            raise OctreeError(rc, lib().svo_last_error().decode())
+        self._h = h
+        self.size, self.brick_dim = size, brick_dim
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().svo_scene_destroy(h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    # ---- construction / update: return 0 (Ok) or an OctreeError code 1..4 ----
+    def _op(self, rc):
+        if rc in (0, 1, 2, 3, 4):
+            return rc
+        raise OctreeError(rc, lib().svo_last_error().decode())
+
+    def set_auto_simplify(self, on):
+        check(lib().svo_set_auto_simplify(self._h, 1 if on else 0))
+
+    def insert(self, pos, albedo=None, user=None):
+        k, a, u = _entry(albedo, user)
+        return self._op(lib().svo_insert(self._h, pos[0], pos[1], pos[2], k, a, u))
+
+    def update(self, pos, albedo=None, user=None):
+        k, a, u = _entry(albedo, user)
+        return self._op(lib().svo_update(self._h, pos[0], pos[1], pos[2], k, a, u))
+
+    def insert_at_lod(self, pos, size, albedo=None, user=None):
+        k, a, u = _entry(albedo, user)
+        return self._op(lib().svo_insert_at_lod(self._h, pos[0], pos[1], pos[2], size, k, a, u))
+
+    def clear(self, pos):
+        return self._op(lib().svo_clear(self._h, pos[0], pos[1], pos[2]))
+
+    def clear_at_lod(self, pos, size):
+        return self._op(lib().svo_clear_at_lod(self._h, pos[0], pos[1], pos[2], size))
+
+    def apply_ops(self, ops):
+        ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
+        done = ctypes.c_uint64()
+        rc = lib().svo_apply_ops(self._h, _vp(_np_ptr(ops)), len(ops), ctypes.byref(done))
+        if rc != 0:
+            raise OctreeError(rc, "apply_ops stopped at op %d: %s" % (done.value, lib().svo_last_error().decode()))
+
+    def get(self, pos):
+        k, a, u = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        check(lib().svo_get(self._h, pos[0], pos[1], pos[2], ctypes.byref(k), ctypes.byref(a), ctypes.byref(u)))
+        return (k.value, a.value, u.value)
+
+    def stats(self):
+        from ._lib import SceneStats
+        s = SceneStats()
+        check(lib().svo_scene_stats_get(self._h, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in SceneStats._fields_}
+
+    def node_record(self, key):
+        rec = (ctypes.c_uint64 * 40)()
+        check(lib().svo_node_record(self._h, key, rec))
+        return tuple(rec)
+
+    def records(self):
+        return [self.node_record(k) for k in range(self.stats()["nodes"])]
+
+    def palette(self, which):
+        n = lib().svo_palette(self._h, which, None, 0)
+        out = np.zeros(n, dtype=np.uint32)
+        lib().svo_palette(self._h, which, _vp(_np_ptr(out)), n)
+        return out
+
+    # ---- device image ----
+    def upload(self, stream=0):
+        check(lib().svo_scene_upload(self._h, _vp(stream)))
+
+    def sync(self, stream=0):
+        check(lib().svo_scene_sync(self._h, _vp(stream)))
+
+    def release_device(self):
+        check(lib().svo_scene_release_device(self._h))
+
+    # ---- the cast ----
+    def cast(self, rays, hits, n, stream=0):
+        """Device cast: ``rays`` / ``hits`` map field names to device pointers (ints)."""
+        r = Rays(*[_vp(rays[k]) for k in ("ox", "oy", "oz", "dx", "dy", "dz")])
+        h = Hits(**{k: _vp(hits.get(k, 0) or 0) for k in HIT_FIELDS})
+        check(lib().svo_cast(self._h, ctypes.byref(r), n, ctypes.byref(h), _vp(stream)))
+
+    def cast_host(self, origins, directions, fields=tuple(HIT_FIELDS), stream=0):
+        """Host-buffer cast (copies in, casts, copies out, synchronises)."""
+        o = np.ascontiguousarray(np.asarray(origins, dtype=np.float32).reshape(-1, 3))
+        d = np.ascontiguousarray(np.asarray(directions, dtype=np.float32).reshape(-1, 3))
+        n = o.shape[0]
+        cols = [np.ascontiguousarray(o[:, k]) for k in range(3)] + [np.ascontiguousarray(d[:, k]) for k in range(3)]
+        out = {k: np.zeros(n, dtype=HIT_FIELDS[k]) for k in fields}
+        r = Rays(*[_vp(c.ctypes.data) for c in cols])
+        h = Hits(**{k: _vp(out[k].ctypes.data) if k in out else None for k in HIT_FIELDS})
+        check(lib().svo_cast_host(self._h, ctypes.byref(r), n, ctypes.byref(h), _vp(stream)))
+        return out
+
+    def cast_host_soa(self, cols, out, stream=0):
+        """Host cast over caller-owned arrays: cols = 6 float32 arrays, out = {field: array}."""
+        n = len(cols[0])
+        r = Rays(*[_vp(c.ctypes.data) for c in cols])
+        h = Hits(**{k: _vp(out[k].ctypes.data) if k in out else None for k in HIT_FIELDS})
+        check(lib().svo_cast_host(self._h, ctypes.byref(r), n, ctypes.byref(h), _vp(stream)))
+
+    def get_by_ray(self, origin, direction):
+        """Octree::get_by_ray for one ray: None or ((kind, rgba, user), point, normal)."""
+        r = self.cast_host([origin], [direction])
+        if r["status"][0] != 1:
+            return None
+        return ((int(r["entry_kind"][0]), int(r["albedo"][0]), int(r["user"][0])),
+                (r["px"][0], r["py"][0], r["pz"][0]), (r["nx"][0], r["ny"][0], r["nz"][0]))
+
+
+class BatchWorkspace:
+    """Owner of the batched cast's device-side item table and work counter."""
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        check(lib().svo_batch_workspace_create(ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().svo_batch_workspace_destroy(h)
+            self._h = None
+
+    def cast(self, items, cfg=None, stream=0):
+        """items: list of (Octree, rays dict, n, hits dict) with device pointers."""
+        from ._lib import BatchItem
+        arr = (BatchItem * len(items))()
+        for i, (scene, rays, n, hits) in enumerate(items):
+            arr[i].scene = scene.handle
+            arr[i].rays = Rays(*[_vp(rays[k]) for k in ("ox", "oy", "oz", "dx", "dy", "dz")])
+            arr[i].n = n
+            arr[i].hits = Hits(**{k: _vp(hits.get(k, 0) or 0) for k in HIT_FIELDS})
+        c = cfg if cfg is not None else LaunchConfig()
+        check(lib().svo_cast_batched(self._h, arr, len(items), ctypes.byref(c), _vp(stream)))
+
+
+def gen_scene(kind, size, brick_dim, seed, occupancy=0.1, spheres=0, octaves=2, base_freq=1.0 / 32,
+              height_lo=0.0, height_hi=96.0, cave_threshold=0.55):
+    """Seeded construction recipe (array of OP_DTYPE ops) of a synthetic scene."""
+    r = SceneRecipe(kind, size, brick_dim, seed, occupancy, spheres, octaves, base_freq, height_lo, height_hi,
+                    cave_threshold)
+    n = ctypes.c_uint64()
+    check(lib().svo_gen_scene(ctypes.byref(r), None, 0, ctypes.byref(n)))
+    ops = np.zeros(n.value, dtype=OP_DTYPE)
+    check(lib().svo_gen_scene(ctypes.byref(r), _vp(_np_ptr(ops)), n.value, ctypes.byref(n)))
+    return ops
+
+
+def _ray_arrays(n):
+    return [np.zeros(n, dtype=np.float32) for _ in range(6)]
+
+
+def gen_camera_rays(eye, target, fov_deg, width, height):
+    """Pinhole camera rays; returns (origins (n,3), directions (n,3)) float32."""
+    cols = _ray_arrays(width * height)
+    e = (ctypes.c_float * 3)(*eye)
+    t = (ctypes.c_float * 3)(*target)
+    check(lib().svo_gen_camera_rays(e, t, ctypes.c_float(fov_deg), width, height, *[_vp(c.ctypes.data) for c in cols]))
+    return np.stack(cols[:3], axis=1), np.stack(cols[3:], axis=1)
+
+
+def gen_sphere_rays(center, radius, n, seed):
+    """Origins uniform on a sphere, directions uniform on S^2."""
+    cols = _ray_arrays(n)
+    c = (ctypes.c_float * 3)(*center)
+    check(lib().svo_gen_sphere_rays(c, ctypes.c_float(radius), n, seed, *[_vp(a.ctypes.data) for a in cols]))
+    return np.stack(cols[:3], axis=1), np.stack(cols[3:], axis=1)

@@ -1,0 +1,120 @@
+"""ctypes loader of libsvo.so (built in-tree by shocovox_gb300/build.py).
+
+Loading fails loudly: if the library cannot be built or loaded, every entry
+point raises; nothing falls back to a CPU path.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+OP_DTYPE = np.dtype([("x", "<u2"), ("y", "<u2"), ("z", "<u2"), ("op", "u1"), ("kind", "u1"),
+                     ("size", "<u4"), ("rgba", "<u4"), ("user", "<u4")])
+assert OP_DTYPE.itemsize == 20
+
+HIT_FIELDS = {
+    "status": np.uint8, "brick_octant": np.uint8, "entry_kind": np.uint8, "node_key": np.uint32,
+    "voxel_index": np.uint32, "pix": np.uint32, "albedo": np.uint32, "user": np.uint32,
+    "px": np.float32, "py": np.float32, "pz": np.float32, "nx": np.float32, "ny": np.float32,
+    "nz": np.float32, "node_visits": np.uint32, "child_reads": np.uint32, "voxel_reads": np.uint32,
+}
+
+
+class Rays(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_void_p) for k in ("ox", "oy", "oz", "dx", "dy", "dz")]
+
+
+class Hits(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_void_p) for k in HIT_FIELDS]
+
+
+class SceneStats(ctypes.Structure):
+    _fields_ = [("nodes", ctypes.c_uint64), ("reserved_nodes", ctypes.c_uint64), ("parted_bricks", ctypes.c_uint64),
+                ("colors", ctypes.c_uint64), ("datas", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64),
+                ("size", ctypes.c_uint32), ("brick_dim", ctypes.c_uint32)]
+
+
+class SceneRecipe(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("size", ctypes.c_uint32), ("brick_dim", ctypes.c_uint32),
+                ("seed", ctypes.c_uint64), ("occupancy", ctypes.c_float), ("spheres", ctypes.c_uint32),
+                ("octaves", ctypes.c_uint32), ("base_freq", ctypes.c_float), ("height_lo", ctypes.c_float),
+                ("height_hi", ctypes.c_float), ("cave_threshold", ctypes.c_float)]
+
+
+class LaunchConfig(ctypes.Structure):
+    _fields_ = [("block", ctypes.c_uint32), ("rays_per_chunk", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
+class BatchItem(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_void_p), ("rays", Rays), ("n", ctypes.c_uint64), ("hits", Hits)]
+
+
+# name -> (restype, argtypes); every symbol of include/svo.h is listed here
+_U32, _U64, _I32, _VP, _F = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_float
+_P = ctypes.POINTER
+SIGNATURES = {
+    "svo_last_error": (ctypes.c_char_p, []),
+    "svo_version": (_I32, []),
+    "svo_scene_create": (_I32, [_U32, _U32, _P(_VP)]),
+    "svo_scene_destroy": (None, [_VP]),
+    "svo_set_auto_simplify": (_I32, [_VP, _I32]),
+    "svo_insert": (_I32, [_VP, _U32, _U32, _U32, _U32, _U32, _U32]),
+    "svo_update": (_I32, [_VP, _U32, _U32, _U32, _U32, _U32, _U32]),
+    "svo_insert_at_lod": (_I32, [_VP, _U32, _U32, _U32, _U32, _U32, _U32, _U32]),
+    "svo_clear": (_I32, [_VP, _U32, _U32, _U32]),
+    "svo_clear_at_lod": (_I32, [_VP, _U32, _U32, _U32, _U32]),
+    "svo_apply_ops": (_I32, [_VP, _VP, _U64, _P(_U64)]),
+    "svo_get": (_I32, [_VP, _U32, _U32, _U32, _P(_U32), _P(_U32), _P(_U32)]),
+    "svo_scene_stats_get": (_I32, [_VP, _P(SceneStats)]),
+    "svo_node_record": (_I32, [_VP, _U64, _P(_U64)]),
+    "svo_palette": (_U64, [_VP, _I32, _VP, _U64]),
+    "svo_scene_upload": (_I32, [_VP, _VP]),
+    "svo_scene_sync": (_I32, [_VP, _VP]),
+    "svo_scene_release_device": (_I32, [_VP]),
+    "svo_cast": (_I32, [_VP, _P(Rays), _U64, _P(Hits), _VP]),
+    "svo_cast_host": (_I32, [_VP, _P(Rays), _U64, _P(Hits), _VP]),
+    "svo_batch_workspace_create": (_I32, [_P(_VP)]),
+    "svo_batch_workspace_destroy": (None, [_VP]),
+    "svo_cast_batched": (_I32, [_VP, _P(BatchItem), _U32, _P(LaunchConfig), _VP]),
+    "svo_gen_scene": (_I32, [_P(SceneRecipe), _VP, _U64, _P(_U64)]),
+    "svo_gen_camera_rays": (_I32, [_P(_F), _P(_F), _F, _U32, _U32, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "svo_gen_sphere_rays": (_I32, [_P(_F), _F, _U64, _U64, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "svo_selftest_luts": (_I32, [_P(_U64), _P(_U32), _P(_U64)]),
+}
+
+
+def lib_path():
+    return _build.LIB
+
+
+def lib():
+    """Loads (building first if needed) libsvo.so and declares its signatures."""
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        if not os.path.exists(path):
+            raise RuntimeError("libsvo.so missing at %s" % path)
+        L = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)  # AttributeError here means the library lacks a declared entry point
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+class SvoError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (svo_status %d)" % (msg, code))
+        self.code = code
+
+
+def check(rc):
+    if rc != 0:
+        raise SvoError(rc, lib().svo_last_error().decode(errors="replace"))
+    return rc

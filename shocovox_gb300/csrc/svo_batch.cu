@@ -1,0 +1,211 @@
+// svo_batch.cu -- batched multi-scene cast: one persistent launch over many
+// (scene, ray batch) items.
+//
+// Work distribution: the rays of all items form one global index space
+// (item prefix sums).  Each warp repeatedly claims `rays_per_chunk`
+// consecutive indices from a device work counter with one atomicAdd, maps
+// every lane's index to its item by binary search over the prefix sums held
+// in shared memory, and casts with the shared per-ray restatement of
+// Octree::get_by_ray (svo_cast.cuh).  Items of different octree sizes and
+// brick dimensions mix freely; a ray's result does not depend on which warp
+// or launch casts it.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "svo_cast.cuh"
+
+namespace svo {
+
+struct BatchItemDev {
+  SceneView scene;
+  RaysView rays;
+  HitsView hits;
+  uint64_t begin;  // first global ray index of the item
+  uint64_t n;
+};
+
+constexpr uint32_t kMaxSharedItems = 1024;  // prefix sums staged in shared memory
+
+template <bool kCount>
+__global__ void batched_kernel(const BatchItemDev* __restrict__ items, uint32_t n_items, uint64_t total,
+                               unsigned long long* __restrict__ counter, uint32_t chunk) {
+  __shared__ uint64_t s_begin[kMaxSharedItems];
+  const uint32_t staged = n_items < kMaxSharedItems ? n_items : kMaxSharedItems;
+  for (uint32_t i = threadIdx.x; i < staged; i += blockDim.x) s_begin[i] = items[i].begin;
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31u;
+  for (;;) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(counter, (unsigned long long)chunk);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (base >= total) break;
+    for (uint32_t k = lane; k < chunk; k += 32) {
+      const uint64_t g = base + k;
+      if (g >= total) break;
+      // largest item with begin <= g (items are sorted by begin)
+      uint32_t lo = 0, hi = n_items - 1;
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        const uint64_t b = mid < kMaxSharedItems ? s_begin[mid] : items[mid].begin;
+        if (b <= g)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      const BatchItemDev& it = items[lo];
+      const uint64_t i = g - it.begin;
+      if (i >= it.n) continue;  // an empty item shares its begin with the next one
+      const RaysView& r = it.rays;
+      HitRecord h;
+      cast_ray<kCount>(it.scene, __ldg(r.ox + i), __ldg(r.oy + i), __ldg(r.oz + i), __ldg(r.dx + i),
+                       __ldg(r.dy + i), __ldg(r.dz + i), h);
+      write_hit(it.scene, it.hits, i, h);
+      if (kCount) {
+        if (it.hits.visits) it.hits.visits[i] = h.visits;
+        if (it.hits.creads) it.hits.creads[i] = h.creads;
+        if (it.hits.vreads) it.hits.vreads[i] = h.vreads;
+      }
+    }
+  }
+}
+
+HitsView hits_view_of(const svo_hits& h) {
+  HitsView v;
+  v.status = h.status;
+  v.octant = h.brick_octant;
+  v.kind = h.entry_kind;
+  v.node = h.node_key;
+  v.voxel = h.voxel_index;
+  v.pix = h.pix;
+  v.albedo = h.albedo;
+  v.user = h.user;
+  v.px = h.px;
+  v.py = h.py;
+  v.pz = h.pz;
+  v.nx = h.nx;
+  v.ny = h.ny;
+  v.nz = h.nz;
+  v.visits = h.node_visits;
+  v.creads = h.child_reads;
+  v.vreads = h.voxel_reads;
+  return v;
+}
+
+}  // namespace svo
+
+// Workspace of the batched cast: device item table + work counter, and a
+// pinned host staging copy of the table.  Grows only when the item count grows.
+struct svo_batch_workspace {
+  svo::BatchItemDev* d_items = nullptr;
+  unsigned long long* d_counter = nullptr;
+  svo::BatchItemDev* h_items = nullptr;  // pinned
+  cudaEvent_t copied = nullptr;           // the last table upload has left h_items
+  uint32_t cap = 0;
+  int sm_count = 0;
+};
+
+using namespace svo;
+
+extern "C" {
+
+svo_status svo_batch_workspace_create(svo_batch_workspace** out) {
+  if (!out) return fail(SVO_ERR_ARGUMENT, "NULL argument");
+  svo_batch_workspace* ws = new svo_batch_workspace();
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ws->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->d_counter, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws->copied, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    cudaFree(ws->d_counter);
+    if (ws->copied) cudaEventDestroy(ws->copied);
+    delete ws;
+    return fail(SVO_ERR_CUDA, std::string("svo_batch_workspace_create: ") + cudaGetErrorString(e));
+  }
+  *out = ws;
+  return SVO_OK;
+}
+
+void svo_batch_workspace_destroy(svo_batch_workspace* ws) {
+  if (!ws) return;
+  cudaFree(ws->d_items);
+  cudaFree(ws->d_counter);
+  cudaFreeHost(ws->h_items);
+  if (ws->copied) cudaEventDestroy(ws->copied);
+  delete ws;
+}
+
+svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items, uint32_t n_items,
+                            const svo_launch_config* cfg, void* stream) {
+  if (!ws || (!items && n_items)) return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: NULL argument");
+  if (n_items == 0) return SVO_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+  SVO_CUDA_TRY(cudaStreamIsCapturing(st, &capturing));
+  const bool in_capture = capturing != cudaStreamCaptureStatusNone;
+  if (n_items > ws->cap) {
+    if (in_capture) return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: workspace must be sized before stream capture");
+    // the previous table may still be read by an in-flight launch on this stream
+    SVO_CUDA_TRY(cudaStreamSynchronize(st));
+    cudaFree(ws->d_items);
+    cudaFreeHost(ws->h_items);
+    ws->d_items = nullptr;
+    ws->h_items = nullptr;
+    ws->cap = 0;
+    const uint32_t cap = std::max<uint32_t>(n_items, 16);
+    SVO_CUDA_TRY(cudaMalloc(&ws->d_items, cap * sizeof(BatchItemDev)));
+    SVO_CUDA_TRY(cudaMallocHost(&ws->h_items, cap * sizeof(BatchItemDev)));
+    ws->cap = cap;
+  } else if (!in_capture) {
+    // the pinned staging table is reused: wait until its previous upload has left it
+    SVO_CUDA_TRY(cudaEventSynchronize(ws->copied));
+  }
+  uint64_t total = 0;
+  bool count = false;
+  for (uint32_t i = 0; i < n_items; ++i) {
+    const svo_batch_item& it = items[i];
+    if (!it.scene) return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: NULL scene");
+    if (!it.scene->dev.valid) return fail(SVO_ERR_NOT_UPLOADED, "svo_cast_batched: scene not uploaded");
+    if (it.n && (!it.rays.ox || !it.rays.oy || !it.rays.oz || !it.rays.dx || !it.rays.dy || !it.rays.dz))
+      return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: NULL ray array");
+    BatchItemDev& d = ws->h_items[i];
+    d.scene = scene_view(it.scene);
+    d.rays = RaysView{it.rays.ox, it.rays.oy, it.rays.oz, it.rays.dx, it.rays.dy, it.rays.dz};
+    d.hits = hits_view_of(it.hits);
+    d.begin = total;
+    d.n = it.n;
+    total += it.n;
+    count |= it.hits.node_visits || it.hits.child_reads || it.hits.voxel_reads;
+  }
+  if (total == 0) return SVO_OK;
+  const uint32_t block = (cfg && cfg->block) ? cfg->block : 128;
+  const uint32_t chunk = (cfg && cfg->rays_per_chunk) ? cfg->rays_per_chunk : 64;
+  if (block % 32 != 0 || block > 1024 || chunk == 0) return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: bad launch config");
+  int per_sm = (cfg && cfg->blocks_per_sm) ? (int)cfg->blocks_per_sm : 0;
+  if (per_sm == 0) {
+    if (count)
+      SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_kernel<true>, block, 0));
+    else
+      SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_kernel<false>, block, 0));
+    per_sm = std::max(per_sm, 1);
+  }
+  const uint64_t warps_needed = (total + chunk - 1) / chunk;
+  uint64_t grid = (uint64_t)ws->sm_count * (uint64_t)per_sm;
+  grid = std::min<uint64_t>(grid, (warps_needed * 32 + block - 1) / block);
+  grid = std::max<uint64_t>(grid, 1);
+  SVO_CUDA_TRY(cudaMemcpyAsync(ws->d_items, ws->h_items, n_items * sizeof(BatchItemDev), cudaMemcpyHostToDevice, st));
+  if (!in_capture) SVO_CUDA_TRY(cudaEventRecord(ws->copied, st));
+  SVO_CUDA_TRY(cudaMemsetAsync(ws->d_counter, 0, sizeof(unsigned long long), st));
+  if (count)
+    batched_kernel<true><<<(unsigned)grid, block, 0, st>>>(ws->d_items, n_items, total, ws->d_counter, chunk);
+  else
+    batched_kernel<false><<<(unsigned)grid, block, 0, st>>>(ws->d_items, n_items, total, ws->d_counter, chunk);
+  SVO_CUDA_TRY(cudaGetLastError());
+  return SVO_OK;
+}
+
+}  // extern "C"

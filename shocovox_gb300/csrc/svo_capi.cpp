@@ -1,0 +1,171 @@
+// svo_capi.cpp -- host-side C ABI of libsvo (construction, update, queries).
+// No exception or panic crosses the boundary: ReferencePanic becomes
+// SVO_ERR_REFERENCE_PANIC, allocation failure SVO_ERR_OUT_OF_MEMORY.
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "svo_internal.h"
+
+namespace svo {
+namespace {
+thread_local std::string g_last_error;
+
+Entry make_entry(uint32_t kind, uint32_t rgba, uint32_t user) {
+  Entry e;
+  e.kind = kind & 3u;
+  e.rgba = (kind & 1u) ? rgba : 0;
+  e.user = (kind & 2u) ? user : 0;
+  return e;
+}
+
+template <class F>
+svo_status guarded(const char* what, F&& f) {
+  try {
+    return f();
+  } catch (const ReferencePanic& p) {
+    return fail(SVO_ERR_REFERENCE_PANIC, std::string(what) + ": the reference panics here (" + p.what() + ")");
+  } catch (const std::bad_alloc&) {
+    return fail(SVO_ERR_OUT_OF_MEMORY, std::string(what) + ": host allocation failed");
+  }
+}
+
+svo_status op_status(int rc, const char* what) {
+  if (rc == 0) return SVO_OK;
+  static const char* names[] = {"ok", "InvalidSize", "InvalidBrickDimension", "InvalidStructure", "InvalidPosition"};
+  return fail(rc, std::string(what) + ": " + (rc < 5 ? names[rc] : "error"));
+}
+}  // namespace
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+svo_status fail(svo_status code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+}  // namespace svo
+
+using namespace svo;
+
+extern "C" {
+
+const char* svo_last_error(void) { return g_last_error.c_str(); }
+int32_t svo_version(void) { return 100; }
+
+svo_status svo_scene_create(uint32_t size, uint32_t brick_dim, svo_scene** out) {
+  if (!out) return fail(SVO_ERR_ARGUMENT, "svo_scene_create: out is NULL");
+  *out = nullptr;
+  return guarded("svo_scene_create", [&]() -> svo_status {
+    svo_scene* s = new svo_scene();
+    int rc = HostOctree::create(size, brick_dim, &s->tree);
+    if (rc != 0) {
+      delete s;
+      return op_status(rc, "Octree::new");
+    }
+    *out = s;
+    return SVO_OK;
+  });
+}
+
+svo_status svo_set_auto_simplify(svo_scene* s, int32_t enabled) {
+  if (!s) return fail(SVO_ERR_ARGUMENT, "NULL scene");
+  s->tree.auto_simplify = enabled != 0;
+  return SVO_OK;
+}
+
+svo_status svo_insert(svo_scene* s, uint32_t x, uint32_t y, uint32_t z, uint32_t kind, uint32_t rgba, uint32_t user) {
+  if (!s) return fail(SVO_ERR_ARGUMENT, "NULL scene");
+  const uint32_t p[3] = {x, y, z};
+  return guarded("insert", [&] { return op_status(s->tree.insert_at_lod(true, p, 1, make_entry(kind, rgba, user)), "insert"); });
+}
+svo_status svo_update(svo_scene* s, uint32_t x, uint32_t y, uint32_t z, uint32_t kind, uint32_t rgba, uint32_t user) {
+  if (!s) return fail(SVO_ERR_ARGUMENT, "NULL scene");
+  const uint32_t p[3] = {x, y, z};
+  return guarded("update", [&] { return op_status(s->tree.insert_at_lod(false, p, 1, make_entry(kind, rgba, user)), "update"); });
+}
+svo_status svo_insert_at_lod(svo_scene* s, uint32_t x, uint32_t y, uint32_t z, uint32_t size, uint32_t kind,
+                             uint32_t rgba, uint32_t user) {
+  if (!s) return fail(SVO_ERR_ARGUMENT, "NULL scene");
+  const uint32_t p[3] = {x, y, z};
+  return guarded("insert_at_lod", [&] {
+    return op_status(s->tree.insert_at_lod(true, p, size, make_entry(kind, rgba, user)), "insert_at_lod");
+  });
+}
+svo_status svo_clear(svo_scene* s, uint32_t x, uint32_t y, uint32_t z) {
+  if (!s) return fail(SVO_ERR_ARGUMENT, "NULL scene");
+  const uint32_t p[3] = {x, y, z};
+  return guarded("clear", [&] { return op_status(s->tree.clear_at_lod(p, 1), "clear"); });
+}
+svo_status svo_clear_at_lod(svo_scene* s, uint32_t x, uint32_t y, uint32_t z, uint32_t size) {
+  if (!s) return fail(SVO_ERR_ARGUMENT, "NULL scene");
+  const uint32_t p[3] = {x, y, z};
+  return guarded("clear_at_lod", [&] { return op_status(s->tree.clear_at_lod(p, size), "clear_at_lod"); });
+}
+
+svo_status svo_apply_ops(svo_scene* s, const svo_op* ops, uint64_t n, uint64_t* n_done) {
+  if (!s || (!ops && n)) return fail(SVO_ERR_ARGUMENT, "svo_apply_ops: NULL argument");
+  uint64_t i = 0;
+  svo_status rc = SVO_OK;
+  for (; i < n; ++i) {
+    const svo_op& o = ops[i];
+    switch (o.op) {
+      case SVO_OP_INSERT: rc = svo_insert(s, o.x, o.y, o.z, o.kind, o.rgba, o.user); break;
+      case SVO_OP_UPDATE: rc = svo_update(s, o.x, o.y, o.z, o.kind, o.rgba, o.user); break;
+      case SVO_OP_INSERT_AT_LOD: rc = svo_insert_at_lod(s, o.x, o.y, o.z, o.size, o.kind, o.rgba, o.user); break;
+      case SVO_OP_CLEAR: rc = svo_clear(s, o.x, o.y, o.z); break;
+      case SVO_OP_CLEAR_AT_LOD: rc = svo_clear_at_lod(s, o.x, o.y, o.z, o.size); break;
+      default: rc = fail(SVO_ERR_ARGUMENT, "svo_apply_ops: unknown op");
+    }
+    if (rc != SVO_OK) break;
+  }
+  if (n_done) *n_done = i;
+  return rc;
+}
+
+svo_status svo_get(svo_scene* s, uint32_t x, uint32_t y, uint32_t z, uint32_t* kind, uint32_t* rgba, uint32_t* user) {
+  if (!s) return fail(SVO_ERR_ARGUMENT, "NULL scene");
+  const uint32_t p[3] = {x, y, z};
+  return guarded("get", [&] {
+    Entry e = s->tree.get(p);
+    if (kind) *kind = e.kind;
+    if (rgba) *rgba = e.rgba;
+    if (user) *user = e.user;
+    return SVO_OK;
+  });
+}
+
+svo_status svo_scene_stats_get(svo_scene* s, svo_scene_stats* out) {
+  if (!s || !out) return fail(SVO_ERR_ARGUMENT, "NULL argument");
+  std::memset(out, 0, sizeof(*out));
+  const HostOctree& t = s->tree;
+  out->nodes = t.nodes();
+  for (auto r : t.reserved) out->reserved_nodes += r;
+  out->parted_bricks = t.arena.live_count();
+  out->colors = t.colors.size();
+  out->datas = t.datas.size();
+  out->size = t.size;
+  out->brick_dim = t.dim;
+  if (s->dev.valid) {
+    const DeviceImage& d = s->dev;
+    out->device_bytes = d.node_cap * sizeof(DevNode) + d.brick_cap * (uint64_t)t.arena.len() * 4 +
+                        d.brick_cap * (uint64_t)(t.arena.len() >= 32 ? t.arena.len() / 32 : 1) * 4 +
+                        (d.color_cap + d.data_cap) * 4;
+  }
+  return SVO_OK;
+}
+
+svo_status svo_node_record(svo_scene* s, uint64_t key, uint64_t rec[40]) {
+  if (!s || !rec) return fail(SVO_ERR_ARGUMENT, "NULL argument");
+  if (key >= s->tree.nodes()) return fail(SVO_ERR_ARGUMENT, "svo_node_record: key out of range");
+  s->tree.node_record(key, rec);
+  return SVO_OK;
+}
+
+uint64_t svo_palette(svo_scene* s, int32_t which, uint32_t* out, uint64_t max) {
+  if (!s) return 0;
+  const auto& p = which == 0 ? s->tree.colors : s->tree.datas;
+  if (out)
+    for (uint64_t i = 0; i < max && i < p.size(); ++i) out[i] = p[i];
+  return p.size();
+}
+
+}  // extern "C"

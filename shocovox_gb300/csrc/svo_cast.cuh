@@ -1,0 +1,416 @@
+// svo_cast.cuh -- device-side restatement of Octree::get_by_ray shared by the
+// plain (one thread per ray) and the batched persistent cast kernels.
+//
+// The cast follows src/raytracing/raytracing_on_cpu.rs:99-565 of shocovox-rs
+// v0.11.1 (MIP maps disabled) operation by operation; compiled with
+// -fmad=false -prec-div=true -prec-sqrt=true -ftz=false so each f32
+// operation rounds exactly like the Rust code.  The look-up tables of
+// src/spatial/lut.rs are evaluated with bit arithmetic (svo_selftest_luts
+// compares them with the reference constants).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "svo_internal.h"
+
+namespace svo {
+
+#define SVO_CUDA_TRY(call)                                                                  \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      return fail(e_ == cudaErrorMemoryAllocation ? SVO_ERR_OUT_OF_MEMORY : SVO_ERR_CUDA,   \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                      \
+  } while (0)
+
+constexpr uint32_t kOob = 8;
+constexpr uint32_t kWorkCap = 1u << 22;  // traversal steps per ray; the reference loops forever past it
+constexpr float kTol = 0.00001f;         // FLOAT_ERROR_TOLERANCE (src/spatial/raytracing/mod.rs:5)
+
+// ------------------------------------------------------------------ Rust f32 semantics
+__device__ __forceinline__ float rmin(float a, float b) { return isnan(a) ? b : (isnan(b) ? a : (b < a ? b : a)); }
+__device__ __forceinline__ float rmax(float a, float b) { return isnan(a) ? b : (isnan(b) ? a : (b > a ? b : a)); }
+__device__ __forceinline__ float rsignum(float x) { return isnan(x) ? x : copysignf(1.0f, x); }
+__device__ __forceinline__ float rclamp(float x, float lo, float hi) {
+  x = (x < lo) ? lo : x;
+  return (x > hi) ? hi : x;
+}
+// `f as i32` (truncate, saturate, NaN -> 0): exactly cvt.rzi.s32.f32
+__device__ __forceinline__ int as_i32(float x) { return __float2int_rz(x); }
+__device__ __forceinline__ int isignum(int v) { return (v > 0) - (v < 0); }
+
+// ------------------------------------------------------------------ look-up tables as arithmetic
+// RAY_TO_NODE_OCCUPANCY_BITMASK_LUT[pos][dir] (src/spatial/lut.rs:33-84, 255-896): the 4x4x4 box
+// between cell pos = x + 4y + 16z and the far corner in direction octant dir.
+__device__ __forceinline__ uint64_t ray_to_node_mask(uint32_t pos, uint32_t dir) {
+  const uint32_t x = pos & 3u, y = (pos >> 2) & 3u, z = (pos >> 4) & 3u;
+  const uint32_t xm = (dir & 1u) ? ((0xFu << x) & 0xFu) : (0xFu >> (3u - x));
+  const uint32_t ym = (dir & 4u) ? ((0xFu << y) & 0xFu) : (0xFu >> (3u - y));
+  const uint32_t zm = (dir & 2u) ? ((0xFu << z) & 0xFu) : (0xFu >> (3u - z));
+  const uint64_t X = (uint64_t)xm * 0x1111111111111111ull;
+  const uint32_t y16 = (ym & 1u) * 0xFu | (ym & 2u) * 0x78u | (ym & 4u) * 0x3C0u | (ym & 8u) * 0x1E00u;
+  const uint64_t Y = (uint64_t)y16 * 0x0001000100010001ull;
+  const uint64_t Z = ((zm & 1u) ? 0xFFFFull : 0ull) | ((zm & 2u) ? 0xFFFF0000ull : 0ull) |
+                     ((zm & 4u) ? 0xFFFF00000000ull : 0ull) | ((zm & 8u) ? 0xFFFF000000000000ull : 0ull);
+  return X & Y & Z;
+}
+// BITMAP_MASK_FOR_OCTANT_LUT (lut.rs:199-208): the 2x2x2 block of octant o
+__device__ __forceinline__ uint64_t octant_mask(uint32_t o) {
+  const uint64_t X = (uint64_t)(3u << (2u * (o & 1u))) * 0x1111111111111111ull;
+  const uint64_t Y = (uint64_t)(0xFFu << (8u * ((o >> 2) & 1u))) * 0x0001000100010001ull;
+  const uint64_t Z = 0xFFFFFFFFull << (32u * ((o >> 1) & 1u));
+  return X & Y & Z;
+}
+// step_octant + OCTANT_STEP_RESULT_LUT (src/spatial/raytracing/mod.rs:68-80, lut.rs:237-253)
+__device__ __forceinline__ uint32_t step_octant(uint32_t o, float sx, float sy, float sz) {
+  const int nx = (int)(o & 1u) + isignum(as_i32(sx));
+  const int ny = (int)((o >> 2) & 1u) + isignum(as_i32(sy));
+  const int nz = (int)((o >> 1) & 1u) + isignum(as_i32(sz));
+  if ((unsigned)nx > 1u || (unsigned)ny > 1u || (unsigned)nz > 1u) return kOob;
+  return (uint32_t)(nx + 2 * nz + 4 * ny);
+}
+// hash_region (src/spatial/math/mod.rs:11-19)
+__device__ __forceinline__ uint32_t hash_region(float ox, float oy, float oz, float half) {
+  return (uint32_t)(ox >= half) + 2u * (uint32_t)(oz >= half) + 4u * (uint32_t)(oy >= half);
+}
+// OCTANT_OFFSET_REGION_LUT (lut.rs:156-197)
+__device__ __forceinline__ float offx(uint32_t o) { return (float)(o & 1u); }
+__device__ __forceinline__ float offy(uint32_t o) { return (float)((o >> 2) & 1u); }
+__device__ __forceinline__ float offz(uint32_t o) { return (float)((o >> 1) & 1u); }
+
+struct Bounds {
+  float x, y, z, s;
+};
+// Cube::child_bounds_for (src/spatial/mod.rs:32-39)
+__device__ __forceinline__ Bounds child_bounds(const Bounds& b, uint32_t o) {
+  const float h = b.s / 2.0f;
+  return Bounds{b.x + offx(o) * h, b.y + offy(o) * h, b.z + offz(o) * h, h};
+}
+
+struct RayState {
+  float dx, dy, dz;     // direction
+  float gx, gy, gz;     // signum(direction)
+  float fx, fy, fz;     // dda scale factors
+  float px, py, pz;     // current point
+};
+
+// dda_step_to_next_sibling (raytracing_on_cpu.rs:124-152)
+__device__ __forceinline__ void dda_step(RayState& r, const Bounds& b, float& sx, float& sy, float& sz) {
+  const float ex = r.px - b.x, ey = r.py - b.y, ez = r.pz - b.z;
+  const float nx = b.s * rmax(r.gx, 0.0f) - r.gx * ex;
+  const float ny = b.s * rmax(r.gy, 0.0f) - r.gy * ey;
+  const float nz = b.s * rmax(r.gz, 0.0f) - r.gz * ez;
+  const float ax = fabsf(nx * r.fx), ay = fabsf(ny * r.fy), az = fabsf(nz * r.fz);
+  const float m = rmin(rmin(ax, ay), az);
+  r.px = r.px + r.dx * m;
+  r.py = r.py + r.dy * m;
+  r.pz = r.pz + r.dz * m;
+  sx = (m == ax) ? r.gx : 0.0f;
+  sy = (m == ay) ? r.gy : 0.0f;
+  sz = (m == az) ? r.gz : 0.0f;
+}
+
+// cube_impact_normal (src/spatial/raytracing/mod.rs:106-134)
+__device__ __forceinline__ void impact_normal(const Bounds& c, float px, float py, float pz, float& nx, float& ny,
+                                              float& nz) {
+  const float h = c.s / 2.0f;
+  const float mx = (c.x + h) - px, my = (c.y + h) - py, mz = (c.z + h) - pz;
+  const float m = rmax(rmax(fabsf(mx), fabsf(my)), fabsf(mz));
+  const float vx = fabsf(mx) == m ? -mx : 0.0f;
+  const float vy = fabsf(my) == m ? -my : 0.0f;
+  const float vz = fabsf(mz) == m ? -mz : 0.0f;
+  const float len = sqrtf((vx * vx + vy * vy) + vz * vz);
+  nx = vx / len;
+  ny = vy / len;
+  nz = vz / len;
+}
+
+struct HitRecord {
+  uint32_t status, octant, node, voxel, pix;
+  float px, py, pz, nx, ny, nz;
+  uint32_t visits, creads, vreads;
+};
+
+enum : uint32_t { kKindNothing = 0, kKindInternal = 1, kKindLeaf = 2, kKindUniform = 3 };
+enum : uint32_t { kBkEmpty = 0, kBkSolid = 1, kBkParted = 2 };
+
+// Outcome of probe_brick: 0 miss, 1 hit, 2 work cap, 3 reference panic.
+template <bool kCount>
+__device__ __forceinline__ uint32_t probe_brick(const SceneView& s, RayState& r, uint32_t bk, uint32_t value,
+                                                const Bounds& bb, HitRecord& h, uint32_t& work) {
+  if (bk == kBkEmpty) return 0;
+  if (bk == kBkSolid) {  // raytracing_on_cpu.rs:269-280
+    h.pix = value;
+    h.voxel = 0xFFFFFFFFu;
+    h.px = r.px;
+    h.py = r.py;
+    h.pz = r.pz;
+    impact_normal(bb, r.px, r.py, r.pz, h.nx, h.ny, h.nz);
+    return 1;
+  }
+  // traverse_brick (raytracing_on_cpu.rs:156-252)
+  const int D = (int)s.dim;
+  const float Df = (float)s.dim;
+  int cx = min(max(as_i32((r.px - bb.x) * Df / bb.s), 0), D - 1);
+  int cy = min(max(as_i32((r.py - bb.y) * Df / bb.s), 0), D - 1);
+  int cz = min(max(as_i32((r.pz - bb.z) * Df / bb.s), 0), D - 1);
+  int flat = cx + cy * D + cz * D * D;
+  const int D3 = D * D * D;
+  const float unit = bb.s / Df;
+  Bounds cur{bb.x + (float)cx * unit, bb.y + (float)cy * unit, bb.z + (float)cz * unit, unit};
+  const uint32_t* bits = s.vbits + (size_t)value * s.vwords;
+  float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+  for (;;) {
+    if (cx < 0 || cx >= D || cy < 0 || cy >= D || cz < 0 || cz >= D) return 0;
+    flat += as_i32(sx) + as_i32(sy) * D + as_i32(sz) * D * D;
+    if (flat < 0 || flat >= D3) return 3;
+    if (kCount) h.vreads++;
+    if (++work > kWorkCap) return 2;
+    if ((__ldg(bits + (flat >> 5)) >> (flat & 31)) & 1u) {
+      const float hs = bb.s / Df;
+      const Bounds hb{bb.x + (float)cx * bb.s / Df, bb.y + (float)cy * bb.s / Df, bb.z + (float)cz * bb.s / Df, hs};
+      h.pix = __ldg(s.voxels + (size_t)value * (size_t)D3 + (size_t)flat);
+      h.voxel = (uint32_t)flat;
+      h.px = r.px;
+      h.py = r.py;
+      h.pz = r.pz;
+      impact_normal(hb, r.px, r.py, r.pz, h.nx, h.ny, h.nz);
+      return 1;
+    }
+    dda_step(r, cur, sx, sy, sz);
+    cur.x = cur.x + sx * unit;
+    cur.y = cur.y + sy * unit;
+    cur.z = cur.z + sz * unit;
+    cx += as_i32(roundf(sx));
+    cy += as_i32(roundf(sy));
+    cz += as_i32(roundf(sz));
+  }
+}
+
+// BITMAP_INDEX_LUT lookup of a clamped bitmap position; false when the reference would index out of bounds.
+__device__ __forceinline__ bool bitmap_index(float bx, float by, float bz, uint32_t& out) {
+  const float fx = floorf(bx), fy = floorf(by), fz = floorf(bz);
+  if (fx >= 4.0f || fy >= 4.0f || fz >= 4.0f) return false;
+  const uint32_t ix = fx > 0.0f ? (uint32_t)fx : 0u;  // `as usize`: NaN and negatives become 0
+  const uint32_t iy = fy > 0.0f ? (uint32_t)fy : 0u;
+  const uint32_t iz = fz > 0.0f ? (uint32_t)fz : 0u;
+  out = ix + 4u * iy + 16u * iz;
+  return true;
+}
+
+// Octree::get_by_ray (raytracing_on_cpu.rs:316-565, MIP maps disabled)
+template <bool kCount>
+__device__ void cast_ray(const SceneView& s, float ox, float oy, float oz, float dx, float dy, float dz, HitRecord& h) {
+  h.status = 0;
+  h.octant = 0;
+  h.node = 0;
+  h.voxel = 0xFFFFFFFFu;
+  h.pix = 0;
+  h.px = h.py = h.pz = h.nx = h.ny = h.nz = 0.0f;
+  if (kCount) h.visits = h.creads = h.vreads = 0;
+
+  RayState r;
+  r.dx = dx;
+  r.dy = dy;
+  r.dz = dz;
+  r.gx = rsignum(dx);
+  r.gy = rsignum(dy);
+  r.gz = rsignum(dz);
+  {  // get_dda_scale_factors (:99-112); powf(q, 2.) == q * q
+    const float a = dz / dx, b = dy / dx, c = dx / dy, d = dz / dy, e = dx / dz, f = dy / dz;
+    r.fx = sqrtf((1.0f + a * a) + b * b);
+    r.fy = sqrtf((c * c + 1.0f) + d * d);
+    r.fz = sqrtf((e * e + 1.0f) + f * f);
+  }
+  const uint32_t dir = hash_region(1.0f + dx, 1.0f + dy, 1.0f + dz, 1.0f);  // hash_direction
+  const float S = s.size;
+  Bounds cb{0.0f, 0.0f, 0.0f, S};
+  uint32_t target;
+  {  // Cube::intersect_ray (src/spatial/raytracing/mod.rs:32-61) on the root bounds
+    const float t1 = (0.0f - ox) / dx, t2 = ((0.0f + S) - ox) / dx;
+    const float t3 = (0.0f - oy) / dy, t4 = ((0.0f + S) - oy) / dy;
+    const float t5 = (0.0f - oz) / dz, t6 = ((0.0f + S) - oz) / dz;
+    const float tmin = rmax(rmax(rmin(t1, t2), rmin(t3, t4)), rmin(t5, t6));
+    const float tmax = rmin(rmin(rmax(t1, t2), rmax(t3, t4)), rmax(t5, t6));
+    if (tmax < 0.0f || tmin > tmax) return;  // miss: target_octant = OOB
+    const float t = tmin < 0.0f ? 0.0f : tmin;
+    r.px = ox + dx * t;
+    r.py = oy + dy * t;
+    r.pz = oz + dz * t;
+    target = hash_region(r.px - 0.0f, r.py - 0.0f, r.pz - 0.0f, S / 2.0f);
+  }
+  uint32_t work = 0;
+  while (target != kOob) {
+    uint32_t cur = 0;
+    cb = Bounds{0.0f, 0.0f, 0.0f, S};
+    // NodeStack<u32, 4> (:20-82) as a shift register: the newest entry in s0
+    uint32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0, count = 1;
+    while (count > 0) {
+      if (++work > kWorkCap) {
+        h.status = 2;
+        return;
+      }
+      if (kCount) h.visits++;
+      const DevNode* nd = s.nodes + cur;
+      const uint4 head = __ldg(reinterpret_cast<const uint4*>(nd));
+      const uint64_t occ = ((uint64_t)head.y << 32) | head.x;
+      const uint32_t meta = head.z;
+      const uint32_t kind = meta & 3u;
+      bool backtrack = kind == kKindUniform;
+      if (target != kOob) {
+        if (kind == kKindUniform) {
+          const uint32_t rc = probe_brick<kCount>(s, r, (meta >> 8) & 3u, __ldg(&nd->slot[0]), cb, h, work);
+          if (rc) {
+            h.status = rc;
+            h.node = cur;
+            h.octant = 0;
+            return;
+          }
+          backtrack = true;
+        } else if (kind == kKindLeaf) {
+          const uint32_t rc = probe_brick<kCount>(s, r, (meta >> (8 + 2 * target)) & 3u, __ldg(&nd->slot[target]),
+                                                  child_bounds(cb, target), h, work);
+          if (rc) {
+            h.status = rc;
+            h.node = cur;
+            h.octant = target;
+            return;
+          }
+        }
+      }
+      float bx = rclamp((r.px - cb.x) * 4.0f / cb.s, kTol, 4.0f - kTol);
+      float by = rclamp((r.py - cb.y) * 4.0f / cb.s, kTol, 4.0f - kTol);
+      float bz = rclamp((r.pz - cb.z) * 4.0f / cb.s, kTol, 4.0f - kTol);
+      uint32_t flat;
+      if (!bitmap_index(bx, by, bz, flat)) {
+        h.status = 3;
+        return;
+      }
+      if (backtrack || target == kOob || occ == 0 || (occ & ray_to_node_mask(flat, dir)) == 0) {
+        // POP (:445-473)
+        s0 = s1;
+        s1 = s2;
+        s2 = s3;
+        --count;
+        if (count > 0) {
+          cur = s0;
+          const float h2 = cb.s / 2.0f, s2x = cb.s * 2.0f;
+          const float pmx = cb.x - fmodf(cb.x, s2x), pmy = cb.y - fmodf(cb.y, s2x), pmz = cb.z - fmodf(cb.z, s2x);
+          const uint32_t ho = hash_region((cb.x + h2) - pmx, (cb.y + h2) - pmy, (cb.z + h2) - pmz, cb.s);
+          float sx, sy, sz;
+          dda_step(r, cb, sx, sy, sz);
+          target = step_octant(ho, sx, sy, sz);
+          cb = Bounds{pmx, pmy, pmz, cb.s * 2.0f};
+        }
+        continue;
+      }
+      Bounds tb = child_bounds(cb, target);
+      uint32_t ck = kind == kKindInternal ? __ldg(&nd->slot[target]) : kInvalidChild;
+      if (kCount) h.creads++;
+      if (ck != kInvalidChild && (occ & octant_mask(target)) != 0) {
+        // PUSH (:484-492)
+        cur = ck;
+        cb = tb;
+        target = hash_region(r.px - tb.x, r.py - tb.y, r.pz - tb.z, tb.s / 2.0f);
+        s3 = s2;
+        s2 = s1;
+        s1 = s0;
+        s0 = ck;
+        count = count < 4 ? count + 1 : 4;
+      } else {
+        // ADVANCE (:494-544)
+        for (;;) {
+          if (++work > kWorkCap) {
+            h.status = 2;
+            return;
+          }
+          float sx, sy, sz;
+          dda_step(r, tb, sx, sy, sz);
+          target = step_octant(target, sx, sy, sz);
+          if (target != kOob) {
+            tb = child_bounds(cb, target);
+            ck = kind == kKindInternal ? __ldg(&nd->slot[target]) : kInvalidChild;
+            if (kCount) h.creads++;
+            bx = bx + sx * 4.0f / cb.s;
+            by = by + sy * 4.0f / cb.s;
+            bz = bz + sz * 4.0f / cb.s;
+            if (!bitmap_index(bx, by, bz, flat)) {
+              h.status = 3;
+              return;
+            }
+          }
+          if (target == kOob) break;
+          if (ck != kInvalidChild && (occ & octant_mask(target)) != 0 && (ray_to_node_mask(flat, dir) & occ) != 0)
+            break;
+          if (kind == kKindLeaf && ((meta >> (8 + 2 * target)) & 3u) != kBkEmpty) break;
+        }
+      }
+    }
+    // restart from the root with a 0.1 nudge (:548-562)
+    r.px = r.px + dx * 0.1f;
+    r.py = r.py + dy * 0.1f;
+    r.pz = r.pz + dz * 0.1f;
+    target = (r.px < S && r.py < S && r.pz < S && r.px > 0.0f && r.py > 0.0f && r.pz > 0.0f)
+                 ? hash_region(r.px, r.py, r.pz, S / 2.0f)
+                 : kOob;
+  }
+}
+
+struct HitsView {
+  uint8_t *status, *octant, *kind;
+  uint32_t *node, *voxel, *pix, *albedo, *user;
+  float *px, *py, *pz, *nx, *ny, *nz;
+  uint32_t *visits, *creads, *vreads;
+};
+
+__device__ __forceinline__ void write_hit(const SceneView& s, const HitsView& o, uint64_t i, HitRecord& h) {
+  uint32_t kind = 0, albedo = 0, user = 0;
+  if (h.status == 1) {  // pix_get_ref (src/octree/node.rs:381-419)
+    const uint32_t c = h.pix & 0xFFFFu, d = h.pix >> 16;
+    if (c < 0xFFFFu) {
+      if (c >= s.n_colors) {
+        h.status = 3;
+      } else {
+        kind |= 1u;
+        albedo = __ldg(s.colors + c);
+      }
+    }
+    if (d != 0xFFFFu) {
+      if (d >= s.n_datas) {
+        h.status = 3;
+      } else {
+        kind |= 2u;
+        user = __ldg(s.datas + d);
+      }
+    }
+  }
+  if (h.status != 1) {
+    h.octant = h.node = h.pix = 0;
+    h.voxel = 0xFFFFFFFFu;
+    h.px = h.py = h.pz = h.nx = h.ny = h.nz = 0.0f;
+    kind = albedo = user = 0;
+  }
+  if (o.status) o.status[i] = (uint8_t)h.status;
+  if (o.octant) o.octant[i] = (uint8_t)h.octant;
+  if (o.kind) o.kind[i] = (uint8_t)kind;
+  if (o.node) o.node[i] = h.node;
+  if (o.voxel) o.voxel[i] = h.voxel;
+  if (o.pix) o.pix[i] = h.pix;
+  if (o.albedo) o.albedo[i] = albedo;
+  if (o.user) o.user[i] = user;
+  if (o.px) o.px[i] = h.px;
+  if (o.py) o.py[i] = h.py;
+  if (o.pz) o.pz[i] = h.pz;
+  if (o.nx) o.nx[i] = h.nx;
+  if (o.ny) o.ny[i] = h.ny;
+  if (o.nz) o.nz[i] = h.nz;
+}
+
+
+struct RaysView {
+  const float *ox, *oy, *oz, *dx, *dy, *dz;
+};
+
+}  // namespace svo

@@ -1,0 +1,378 @@
+// svo_device.cu -- device image of a scene and the plain get_by_ray cast of libsvo (sm_103a).
+//
+// The device image: 64-byte node records, a brick arena of
+// PaletteIndexValues, one occupancy bit per voxel and the two palettes,
+// uploaded once and then synced in place from the host octree's dirty
+// flags.  The plain cast runs one thread per ray (svo_cast.cuh holds the
+// per-ray restatement of Octree::get_by_ray).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include "svo_cast.cuh"
+
+namespace svo {
+
+template <bool kCount>
+__global__ void __launch_bounds__(128) cast_kernel(SceneView s, RaysView rays, HitsView out, uint64_t n) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  HitRecord h;
+  cast_ray<kCount>(s, __ldg(rays.ox + i), __ldg(rays.oy + i), __ldg(rays.oz + i), __ldg(rays.dx + i),
+                   __ldg(rays.dy + i), __ldg(rays.dz + i), h);
+  write_hit(s, out, i, h);
+  if (kCount) {
+    if (out.visits) out.visits[i] = h.visits;
+    if (out.creads) out.creads[i] = h.creads;
+    if (out.vreads) out.vreads[i] = h.vreads;
+  }
+}
+
+// ------------------------------------------------------------------ device image
+SceneView scene_view(const svo_scene* sc) {
+  const DeviceImage& d = sc->dev;
+  SceneView v;
+  v.nodes = d.nodes;
+  v.voxels = d.voxels;
+  v.vbits = d.vbits;
+  v.colors = d.colors;
+  v.datas = d.datas;
+  v.n_nodes = (uint32_t)d.n_nodes;
+  v.n_colors = (uint32_t)d.n_colors;
+  v.n_datas = (uint32_t)d.n_datas;
+  v.dim = sc->tree.dim;
+  const uint32_t len = sc->tree.arena.len();
+  v.vwords = len >= 32 ? len / 32 : 1;
+  v.size = (float)sc->tree.size;
+  return v;
+}
+
+namespace {
+
+uint32_t vwords_of(const HostOctree& t) { return t.arena.len() >= 32 ? t.arena.len() / 32 : 1; }
+
+void build_node(const HostOctree& t, size_t k, DevNode& n) {
+  std::memset(&n, 0, sizeof(n));
+  for (auto& v : n.slot) v = kInvalidChild;
+  if (!t.reserved[k]) return;
+  const uint32_t kind = t.kind[k];
+  n.ocbits = t.stored_occupied_bits(k);
+  n.meta = kind | (1u << 2);
+  if (kind == kInternal) {
+    if (t.ch_kind[k] == kChildren)
+      for (int i = 0; i < 8; ++i) {
+        const uint32_t c = t.ch[k * 8 + i];
+        n.slot[i] = t.key_valid(c) ? c : kInvalidChild;
+      }
+  } else if (kind == kLeaf || kind == kUniform) {
+    const int nb = kind == kLeaf ? 8 : 1;
+    for (int i = 0; i < nb; ++i) {
+      const BrickRef& b = t.bricks[k * 8 + i];
+      n.meta |= (uint32_t)b.kind << (8 + 2 * i);
+      n.slot[i] = b.kind == kBrickEmpty ? 0u : b.v;
+    }
+  }
+}
+
+void build_vbits(const HostOctree& t, uint32_t slot, uint32_t* out) {
+  const uint32_t W = vwords_of(t), len = t.arena.len();
+  std::memset(out, 0, sizeof(uint32_t) * W);
+  if (!t.arena.live(slot)) return;
+  const uint32_t* v = t.arena.at(slot);
+  for (uint32_t f = 0; f < len; ++f)
+    if (!t.pix_empty(v[f])) out[f >> 5] |= 1u << (f & 31);
+}
+
+void free_device(DeviceImage& d) {
+  cudaFree(d.nodes);
+  cudaFree(d.voxels);
+  cudaFree(d.vbits);
+  cudaFree(d.colors);
+  cudaFree(d.datas);
+  d.nodes = nullptr;
+  d.voxels = d.vbits = d.colors = d.datas = nullptr;
+  d.node_cap = d.brick_cap = d.color_cap = d.data_cap = 0;
+  d.valid = false;
+}
+
+svo_status full_upload(svo_scene* sc, cudaStream_t st) {
+  HostOctree& t = sc->tree;
+  DeviceImage& d = sc->dev;
+  free_device(d);
+  const uint64_t nn = t.nodes(), nb = std::max<uint64_t>(1, t.arena.slots());
+  const uint64_t nc = std::max<uint64_t>(1, t.colors.size()), ndt = std::max<uint64_t>(1, t.datas.size());
+  // headroom so that later in-place syncs rarely need a new allocation
+  d.node_cap = nn + nn / 4 + 64;
+  d.brick_cap = nb + nb / 4 + 16;
+  d.color_cap = nc + nc / 4 + 64;
+  d.data_cap = ndt + ndt / 4 + 64;
+  const uint32_t W = vwords_of(t), len = t.arena.len();
+  try {
+    d.host_nodes.assign(nn, DevNode{});
+    for (uint64_t k = 0; k < nn; ++k) build_node(t, k, d.host_nodes[k]);
+    d.host_vbits.assign(t.arena.slots() * (size_t)W, 0u);
+    for (uint32_t sl = 0; sl < t.arena.slots(); ++sl) build_vbits(t, sl, &d.host_vbits[(size_t)sl * W]);
+  } catch (const ReferencePanic& p) {
+    return fail(SVO_ERR_REFERENCE_PANIC, std::string("upload: ") + p.what());
+  }
+  SVO_CUDA_TRY(cudaMalloc(&d.nodes, d.node_cap * sizeof(DevNode)));
+  SVO_CUDA_TRY(cudaMalloc(&d.voxels, d.brick_cap * (size_t)len * 4));
+  SVO_CUDA_TRY(cudaMalloc(&d.vbits, d.brick_cap * (size_t)W * 4));
+  SVO_CUDA_TRY(cudaMalloc(&d.colors, d.color_cap * 4));
+  SVO_CUDA_TRY(cudaMalloc(&d.datas, d.data_cap * 4));
+  SVO_CUDA_TRY(cudaMemcpyAsync(d.nodes, d.host_nodes.data(), nn * sizeof(DevNode), cudaMemcpyHostToDevice, st));
+  if (t.arena.slots()) {
+    SVO_CUDA_TRY(cudaMemcpyAsync(d.voxels, t.arena.raw().data(), (size_t)t.arena.slots() * len * 4,
+                                 cudaMemcpyHostToDevice, st));
+    SVO_CUDA_TRY(cudaMemcpyAsync(d.vbits, d.host_vbits.data(), d.host_vbits.size() * 4, cudaMemcpyHostToDevice, st));
+  }
+  if (!t.colors.empty())
+    SVO_CUDA_TRY(cudaMemcpyAsync(d.colors, t.colors.data(), t.colors.size() * 4, cudaMemcpyHostToDevice, st));
+  if (!t.datas.empty())
+    SVO_CUDA_TRY(cudaMemcpyAsync(d.datas, t.datas.data(), t.datas.size() * 4, cudaMemcpyHostToDevice, st));
+  // pageable sources: the copies are staged before cudaMemcpyAsync returns, but
+  // the mirrors must stay valid until then, which they do (they live in the scene)
+  d.n_nodes = nn;
+  d.n_bricks = t.arena.slots();
+  d.n_colors = t.colors.size();
+  d.n_datas = t.datas.size();
+  std::fill(t.node_dirty.begin(), t.node_dirty.end(), 0);
+  std::fill(t.arena.dirty().begin(), t.arena.dirty().end(), 0);
+  t.colors_synced = t.colors.size();
+  t.datas_synced = t.datas.size();
+  t.structure_grew = false;
+  d.valid = true;
+  return SVO_OK;
+}
+
+// Copies runs of flagged elements [i, j) with one cudaMemcpyAsync per run.
+template <class F>
+svo_status copy_runs(std::vector<uint8_t>& flags, uint64_t limit, F&& copy) {
+  uint64_t i = 0;
+  while (i < limit) {
+    if (!flags[i]) {
+      ++i;
+      continue;
+    }
+    uint64_t j = i;
+    while (j < limit && flags[j]) flags[j++] = 0;
+    svo_status rc = copy(i, j);
+    if (rc != SVO_OK) return rc;
+    i = j;
+  }
+  return SVO_OK;
+}
+
+svo_status incremental_sync(svo_scene* sc, cudaStream_t st) {
+  HostOctree& t = sc->tree;
+  DeviceImage& d = sc->dev;
+  const uint64_t nn = t.nodes();
+  if (nn > d.node_cap || t.arena.slots() > d.brick_cap || t.colors.size() > d.color_cap || t.datas.size() > d.data_cap)
+    return full_upload(sc, st);
+  const uint32_t W = vwords_of(t), len = t.arena.len();
+  try {
+    d.host_nodes.resize(nn);
+    for (uint64_t k = 0; k < nn; ++k)
+      if (t.node_dirty[k]) build_node(t, k, d.host_nodes[k]);
+    d.host_vbits.resize((size_t)t.arena.slots() * W, 0u);
+    auto& bd = t.arena.dirty();
+    for (uint32_t sl = 0; sl < t.arena.slots(); ++sl)
+      if (bd[sl]) build_vbits(t, sl, &d.host_vbits[(size_t)sl * W]);
+  } catch (const ReferencePanic& p) {
+    return fail(SVO_ERR_REFERENCE_PANIC, std::string("sync: ") + p.what());
+  }
+  svo_status rc = copy_runs(t.node_dirty, nn, [&](uint64_t a, uint64_t b) -> svo_status {
+    SVO_CUDA_TRY(cudaMemcpyAsync(d.nodes + a, d.host_nodes.data() + a, (b - a) * sizeof(DevNode),
+                                 cudaMemcpyHostToDevice, st));
+    return SVO_OK;
+  });
+  if (rc != SVO_OK) return rc;
+  rc = copy_runs(t.arena.dirty(), t.arena.slots(), [&](uint64_t a, uint64_t b) -> svo_status {
+    SVO_CUDA_TRY(cudaMemcpyAsync(d.voxels + a * len, t.arena.raw().data() + a * len, (b - a) * len * 4,
+                                 cudaMemcpyHostToDevice, st));
+    SVO_CUDA_TRY(cudaMemcpyAsync(d.vbits + a * W, d.host_vbits.data() + a * W, (b - a) * W * 4,
+                                 cudaMemcpyHostToDevice, st));
+    return SVO_OK;
+  });
+  if (rc != SVO_OK) return rc;
+  if (t.colors.size() > t.colors_synced)
+    SVO_CUDA_TRY(cudaMemcpyAsync(d.colors + t.colors_synced, t.colors.data() + t.colors_synced,
+                                 (t.colors.size() - t.colors_synced) * 4, cudaMemcpyHostToDevice, st));
+  if (t.datas.size() > t.datas_synced)
+    SVO_CUDA_TRY(cudaMemcpyAsync(d.datas + t.datas_synced, t.datas.data() + t.datas_synced,
+                                 (t.datas.size() - t.datas_synced) * 4, cudaMemcpyHostToDevice, st));
+  t.colors_synced = t.colors.size();
+  t.datas_synced = t.datas.size();
+  d.n_nodes = nn;
+  d.n_bricks = t.arena.slots();
+  d.n_colors = t.colors.size();
+  d.n_datas = t.datas.size();
+  return SVO_OK;
+}
+
+HitsView hits_view(const svo_hits* h) {
+  HitsView v;
+  v.status = h->status;
+  v.octant = h->brick_octant;
+  v.kind = h->entry_kind;
+  v.node = h->node_key;
+  v.voxel = h->voxel_index;
+  v.pix = h->pix;
+  v.albedo = h->albedo;
+  v.user = h->user;
+  v.px = h->px;
+  v.py = h->py;
+  v.pz = h->pz;
+  v.nx = h->nx;
+  v.ny = h->ny;
+  v.nz = h->nz;
+  v.visits = h->node_visits;
+  v.creads = h->child_reads;
+  v.vreads = h->voxel_reads;
+  return v;
+}
+
+svo_status launch_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_hits* hits, cudaStream_t st) {
+  if (n == 0) return SVO_OK;
+  const SceneView v = scene_view(sc);
+  RaysView rv{rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz};
+  const HitsView hv = hits_view(hits);
+  const bool count = hits->node_visits || hits->child_reads || hits->voxel_reads;
+  const unsigned block = 128;
+  const uint64_t grid = (n + block - 1) / block;
+  if (grid > 0x7FFFFFFFull) return fail(SVO_ERR_ARGUMENT, "svo_cast: too many rays for one launch");
+  if (count)
+    cast_kernel<true><<<(unsigned)grid, block, 0, st>>>(v, rv, hv, n);
+  else
+    cast_kernel<false><<<(unsigned)grid, block, 0, st>>>(v, rv, hv, n);
+  SVO_CUDA_TRY(cudaGetLastError());
+  return SVO_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ LUT self-test kernel
+__global__ void lut_kernel(uint64_t* rtn, uint32_t* step, uint64_t* mask) {
+  const uint32_t t = threadIdx.x;
+  if (t < 512) rtn[t] = ray_to_node_mask(t >> 3, t & 7u);
+  if (t < 8) mask[t] = octant_mask(t);
+  if (t < 27) {  // OCTANT_STEP_RESULT_LUT[x][y][z] packs 8 octants x 4 bits
+    const int x = (int)(t / 9) - 1, y = (int)((t / 3) % 3) - 1, z = (int)(t % 3) - 1;
+    uint32_t packed = 0;
+    for (uint32_t o = 0; o < 8; ++o) packed |= (step_octant(o, (float)x, (float)y, (float)z) & 0xFu) << (4 * o);
+    step[t] = packed;
+  }
+}
+
+}  // namespace svo
+
+using namespace svo;
+
+extern "C" {
+
+svo_status svo_scene_upload(svo_scene* sc, void* stream) {
+  if (!sc) return fail(SVO_ERR_ARGUMENT, "NULL scene");
+  return full_upload(sc, (cudaStream_t)stream);
+}
+
+svo_status svo_scene_sync(svo_scene* sc, void* stream) {
+  if (!sc) return fail(SVO_ERR_ARGUMENT, "NULL scene");
+  if (!sc->dev.valid) return full_upload(sc, (cudaStream_t)stream);
+  return incremental_sync(sc, (cudaStream_t)stream);
+}
+
+svo_status svo_scene_release_device(svo_scene* sc) {
+  if (!sc) return fail(SVO_ERR_ARGUMENT, "NULL scene");
+  free_device(sc->dev);
+  cudaFree(sc->dev.ws);
+  sc->dev.ws = nullptr;
+  sc->dev.ws_bytes = 0;
+  std::fill(sc->tree.node_dirty.begin(), sc->tree.node_dirty.end(), 1);
+  std::fill(sc->tree.arena.dirty().begin(), sc->tree.arena.dirty().end(), 1);
+  return SVO_OK;
+}
+
+void svo_scene_destroy(svo_scene* sc) {
+  if (!sc) return;
+  free_device(sc->dev);
+  cudaFree(sc->dev.ws);
+  delete sc;
+}
+
+svo_status svo_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_hits* hits, void* stream) {
+  if (!sc || !rays || !hits) return fail(SVO_ERR_ARGUMENT, "svo_cast: NULL argument");
+  if (!sc->dev.valid) return fail(SVO_ERR_NOT_UPLOADED, "svo_cast: scene has no device image (svo_scene_upload)");
+  if (n && (!rays->ox || !rays->oy || !rays->oz || !rays->dx || !rays->dy || !rays->dz))
+    return fail(SVO_ERR_ARGUMENT, "svo_cast: NULL ray array");
+  return launch_cast(sc, rays, n, hits, (cudaStream_t)stream);
+}
+
+svo_status svo_cast_host(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_hits* hits, void* stream) {
+  if (!sc || !rays || !hits) return fail(SVO_ERR_ARGUMENT, "svo_cast_host: NULL argument");
+  if (!sc->dev.valid) return fail(SVO_ERR_NOT_UPLOADED, "svo_cast_host: scene has no device image");
+  if (n == 0) return SVO_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  // workspace layout: 6 ray arrays then one slot per hit field (bytes per element below)
+  static const size_t kFieldBytes[17] = {1, 1, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4};
+  void* const* host_fields = reinterpret_cast<void* const*>(hits);
+  size_t need = 6 * n * 4;
+  for (int f = 0; f < 17; ++f)
+    if (host_fields[f]) need += ((kFieldBytes[f] * n + 255) / 256) * 256;
+  if (need > sc->dev.ws_bytes) {
+    cudaFree(sc->dev.ws);
+    sc->dev.ws = nullptr;
+    sc->dev.ws_bytes = 0;
+    SVO_CUDA_TRY(cudaMalloc(&sc->dev.ws, need));
+    sc->dev.ws_bytes = need;
+  }
+  char* base = static_cast<char*>(sc->dev.ws);
+  float* dr[6];
+  const float* hr[6] = {rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz};
+  for (int a = 0; a < 6; ++a) {
+    dr[a] = reinterpret_cast<float*>(base + (size_t)a * n * 4);
+    SVO_CUDA_TRY(cudaMemcpyAsync(dr[a], hr[a], n * 4, cudaMemcpyHostToDevice, st));
+  }
+  svo_hits dh;
+  std::memset(&dh, 0, sizeof(dh));
+  void** dev_fields = reinterpret_cast<void**>(&dh);
+  size_t off = 6 * n * 4;
+  for (int f = 0; f < 17; ++f)
+    if (host_fields[f]) {
+      dev_fields[f] = base + off;
+      off += ((kFieldBytes[f] * n + 255) / 256) * 256;
+    }
+  svo_rays drays{dr[0], dr[1], dr[2], dr[3], dr[4], dr[5]};
+  svo_status rc = launch_cast(sc, &drays, n, &dh, st);
+  if (rc != SVO_OK) return rc;
+  for (int f = 0; f < 17; ++f)
+    if (host_fields[f])
+      SVO_CUDA_TRY(cudaMemcpyAsync(host_fields[f], dev_fields[f], kFieldBytes[f] * n, cudaMemcpyDeviceToHost, st));
+  SVO_CUDA_TRY(cudaStreamSynchronize(st));
+  return SVO_OK;
+}
+
+// Runs the device-side look-up-table arithmetic and copies the tables back
+// (RAY_TO_NODE_OCCUPANCY_BITMASK_LUT [64][8], OCTANT_STEP_RESULT_LUT [3][3][3],
+// BITMAP_MASK_FOR_OCTANT_LUT [8]) so tests can compare them with the reference.
+svo_status svo_selftest_luts(uint64_t* ray_to_node, uint32_t* octant_step, uint64_t* octant_masks) {
+  if (!ray_to_node || !octant_step || !octant_masks) return fail(SVO_ERR_ARGUMENT, "NULL argument");
+  uint64_t *d_rtn = nullptr, *d_mask = nullptr;
+  uint32_t* d_step = nullptr;
+  SVO_CUDA_TRY(cudaMalloc(&d_rtn, 512 * 8));
+  SVO_CUDA_TRY(cudaMalloc(&d_mask, 8 * 8));
+  SVO_CUDA_TRY(cudaMalloc(&d_step, 27 * 4));
+  lut_kernel<<<1, 512>>>(d_rtn, d_step, d_mask);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(ray_to_node, d_rtn, 512 * 8, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(octant_step, d_step, 27 * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(octant_masks, d_mask, 8 * 8, cudaMemcpyDeviceToHost);
+  cudaFree(d_rtn);
+  cudaFree(d_mask);
+  cudaFree(d_step);
+  if (e != cudaSuccess) return fail(SVO_ERR_CUDA, std::string("svo_selftest_luts: ") + cudaGetErrorString(e));
+  return SVO_OK;
+}
+
+}  // extern "C"

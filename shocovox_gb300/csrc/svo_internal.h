@@ -1,0 +1,68 @@
+// svo_internal.h -- definitions shared by libsvo's translation units: the
+// scene handle, the device image layout and the error reporting helpers.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/svo.h"
+#include "svo_octree.h"
+
+namespace svo {
+
+// One node of the device image: 64 bytes, 64-byte aligned, so a node visit
+// reads one 32-byte sector for (ocbits, meta) and one for the 8 slots.
+struct alignas(64) DevNode {
+  uint64_t ocbits;   // stored_occupied_bits (src/octree/detail.rs:508-528)
+  uint32_t meta;     // [1:0] content kind, [2] reserved, [23:8] 2-bit brick kind per octant
+  uint32_t pad0;
+  uint32_t pad1[4];
+  uint32_t slot[8];  // Internal: child key or kInvalidChild; Leaf: brick per octant; UniformLeaf: slot[0]
+};
+static_assert(sizeof(DevNode) == 64, "DevNode must be 64 bytes");
+
+constexpr uint32_t kInvalidChild = 0xFFFFFFFFu;
+
+// Everything a cast kernel needs to read one scene (all device pointers).
+struct SceneView {
+  const DevNode* nodes;
+  const uint32_t* voxels;  // brick arena: slot * D^3 PaletteIndexValues
+  const uint32_t* vbits;   // per slot: vwords words, bit f set <=> voxel f is not empty
+  const uint32_t* colors;  // colour palette, 0xRRGGBBAA
+  const uint32_t* datas;   // user-data palette
+  uint32_t n_nodes, n_colors, n_datas;
+  uint32_t dim;     // brick dimension D
+  uint32_t vwords;  // max(1, D^3 / 32)
+  float size;       // octree size
+};
+
+struct DeviceImage {
+  DevNode* nodes = nullptr;
+  uint32_t* voxels = nullptr;
+  uint32_t* vbits = nullptr;
+  uint32_t* colors = nullptr;
+  uint32_t* datas = nullptr;
+  uint64_t node_cap = 0, brick_cap = 0, color_cap = 0, data_cap = 0;
+  uint64_t n_nodes = 0, n_bricks = 0, n_colors = 0, n_datas = 0;
+  bool valid = false;
+  // host mirror of the node records and voxel bits (source of in-place syncs)
+  std::vector<DevNode> host_nodes;
+  std::vector<uint32_t> host_vbits;
+  // workspace of svo_cast_host (device buffers, grown on demand)
+  void* ws = nullptr;
+  uint64_t ws_bytes = 0;
+};
+
+}  // namespace svo
+
+struct svo_scene {
+  svo::HostOctree tree;
+  svo::DeviceImage dev;
+};
+
+namespace svo {
+void set_error(const std::string& msg);
+svo_status fail(svo_status code, const std::string& msg);
+SceneView scene_view(const svo_scene* s);
+}  // namespace svo

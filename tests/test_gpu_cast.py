@@ -1,0 +1,241 @@
+"""GPU parity: libsvo's sm_103a cast against the oracle's CPU restatement of get_by_ray.
+
+Hit identity (status, node key, brick octant, voxel index, PaletteIndexValues,
+entry kind, albedo, user data) must match exactly; impact point and normal
+within 1e-4 voxel units (TOL below).  Counters of the instrumented cast
+(node visits, child reads, voxel reads) must match exactly too.
+"""
+import json
+import os
+import zlib
+
+import numpy as np
+import pytest
+
+import shocovox_gb300 as svo
+from helpers import (ALBEDO, GOLDEN, INSERT, normalized, ops_from, ray_of, scene_brick_boundary, scene_dot_cube,
+                     scene_floor, scene_stairs)
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4  # voxel units, impact point and normal
+INT_FIELDS = ["status", "brick_octant", "entry_kind", "node_key", "voxel_index", "pix", "albedo", "user"]
+FLOAT_FIELDS = ["px", "py", "pz", "nx", "ny", "nz"]
+COUNTERS = ["node_visits", "child_reads", "voxel_reads"]
+
+
+def assert_same_hits(gpu, cpu, counters=False, label=""):
+    n = len(cpu["status"])
+    for f in INT_FIELDS + (COUNTERS if counters else []):
+        bad = np.nonzero(gpu[f] != cpu[f])[0]
+        assert len(bad) == 0, "%s: %s differs on %d/%d rays, first %d: gpu %s cpu %s" % (
+            label, f, len(bad), n, bad[0], gpu[f][bad[0]], cpu[f][bad[0]])
+    for f in FLOAT_FIELDS:
+        d = np.abs(gpu[f].astype(np.float64) - cpu[f].astype(np.float64))
+        assert np.all(d <= TOL), "%s: %s max diff %g" % (label, f, d.max())
+
+
+def both(oracle_mod, size, dim, ops):
+    o = oracle_mod.Tree(size, dim)
+    o.apply_ops(ops)
+    p = svo.Octree(size, dim)
+    p.apply_ops(ops)
+    p.upload()
+    return o, p
+
+
+def test_device_luts_match_reference_constants():
+    import ctypes
+    with open(os.path.join(GOLDEN, "luts.json")) as f:
+        g = json.load(f)
+    rtn = (ctypes.c_uint64 * 512)()
+    step = (ctypes.c_uint32 * 27)()
+    mask = (ctypes.c_uint64 * 8)()
+    assert svo.lib().svo_selftest_luts(rtn, step, mask) == 0
+    assert list(rtn) == [int(v, 16) for v in g["RAY_TO_NODE_OCCUPANCY_BITMASK_LUT"]]
+    assert list(step) == g["OCTANT_STEP_RESULT_LUT"]
+    assert list(mask) == [int(v, 16) for v in g["BITMAP_MASK_FOR_OCTANT_LUT"]]
+
+
+KNOWN = [
+    ("test_edge_case_unreachable", scene_stairs),
+    ("test_edge_case_zero_advance", scene_stairs),
+    ("test_edge_case_loop_stuck", lambda: scene_stairs(True)),
+    ("test_edge_case_empty_line_in_middle", lambda: (4, 1, ops_from([(INSERT, 2, 1, 1, ALBEDO, 3, 0)]))),
+    ("test_edge_case_edge_raycast", scene_floor),
+    ("test_edge_case_voxel_corner", scene_floor),
+    ("test_edge_case_bottom_edge", scene_floor),
+    ("test_edge_case_overlapping_voxels",
+     lambda: (4, 1, ops_from([(INSERT, 0, 0, 0, 2, 0, 5), (INSERT, 1, 0, 0, ALBEDO, 6, 0)]))),
+    ("test_edge_case_brick_undetected", lambda: scene_floor(8, 4)),
+    ("test_edge_case_brick_traversal_error", lambda: (8, 2, ops_from([(INSERT, 0, 0, 0, ALBEDO, 0xFF, 0)]))),
+    ("test_edge_case_brick_boundary_error", scene_brick_boundary),
+    ("test_edge_case_cube_flaps", lambda: scene_dot_cube(32, 1, True, False)),
+    ("test_edge_case_context_bleed", lambda: scene_dot_cube(32, 1, False, True)),
+]
+
+
+@pytest.mark.parametrize("name,scene", KNOWN, ids=[k[0] for k in KNOWN])
+def test_known_answer_rays(oracle_mod, name, scene):
+    o, p = both(oracle_mod, *scene())
+    orig, d = ray_of(name)
+    # the known ray plus a fan of nearby rays through the same scene
+    rng = np.random.default_rng(zlib.crc32(name.encode()))
+    dirs = np.concatenate([d[None], d[None] + rng.normal(0, 0.05, size=(255, 3)).astype(np.float32)])
+    dirs = np.stack([normalized(v) for v in dirs])
+    origins = np.repeat(orig[None], len(dirs), axis=0)
+    assert_same_hits(p.cast_host(origins, dirs), o.cast(origins, dirs), counters=True, label=name)
+
+
+def test_known_answer_expectations_on_gpu(oracle_mod):
+    # tests.rs:597-628 and :731-770 asserted directly on the GPU results
+    o, p = both(oracle_mod, 8, 2, ops_from([(INSERT, x, y, z, ALBEDO, z, 0)
+                                             for x in range(1, 8) for y in range(1, 8) for z in range(1, 8)]))
+    hit = p.get_by_ray(*ray_of("test_edge_case_detailed_brick_z_edge_error"))
+    assert hit is not None and hit[0] == (1, 1, 0) and tuple(hit[2]) == (0.0, 0.0, -1.0)
+    o, p = both(oracle_mod, *scene_dot_cube(32, 1, True, False))
+    assert p.get_by_ray(*ray_of("test_edge_case_cube_flaps")) is None
+    o, p = both(oracle_mod, 512, 1, ops_from([(INSERT, 0, 0, 0, ALBEDO, 0xEE, 0), (INSERT, 511, 511, 511, ALBEDO, 0xFF, 0)]))
+    origin = np.array([0, 5, -1], dtype=np.float32)
+    hit = p.get_by_ray(origin, normalized(np.array([511.5, 511.5, 511.5], dtype=np.float32) - origin))
+    assert hit is not None and hit[0] == (1, 0xFF, 0)
+
+
+def random_rays(rng, size, n, inside_frac=0.3):
+    """Mixed rays: from outside towards the volume, from inside, and axis-aligned ones."""
+    o = np.empty((n, 3), dtype=np.float32)
+    d = np.empty((n, 3), dtype=np.float32)
+    for i in range(n):
+        if rng.random() < inside_frac:
+            o[i] = rng.uniform(0, size, 3)
+        else:
+            o[i] = rng.uniform(-0.5 * size, 1.5 * size, 3)
+        t = rng.uniform(0, size, 3)
+        if rng.random() < 0.05:  # axis-aligned direction (zero components)
+            v = np.zeros(3, dtype=np.float32)
+            v[rng.integers(0, 3)] = rng.choice([-1.0, 1.0])
+        elif rng.random() < 0.05:  # through integer lattice points (voxel corners and edges)
+            o[i] = np.round(o[i])
+            v = np.round(t) - o[i]
+        else:
+            v = t - o[i]
+        if not np.any(v):
+            v = np.array([0, -1, 0], dtype=np.float32)
+        d[i] = normalized(v.astype(np.float32))
+    return o, d
+
+
+@pytest.mark.parametrize("kind,size,dim", [(0, 32, 1), (0, 64, 2), (0, 128, 4), (1, 128, 8), (2, 128, 8),
+                                           (3, 64, 2), (3, 128, 4), (3, 64, 16)])
+def test_generated_scenes_random_rays(oracle_mod, kind, size, dim):
+    ops = svo.gen_scene(kind, size, dim, seed=77 + size + dim, occupancy=0.12, spheres=6, octaves=2,
+                        base_freq=1.0 / 16, height_lo=2.0, height_hi=size * 0.4, cave_threshold=0.55)
+    o, p = both(oracle_mod, size, dim, ops)
+    rng = np.random.default_rng(size * 100 + dim)
+    origins, dirs = random_rays(rng, size, 4000)
+    assert_same_hits(p.cast_host(origins, dirs), o.cast(origins, dirs, threads=8), counters=True,
+                     label="kind%d %d/%d" % (kind, size, dim))
+
+
+def test_small_heightfield_camera_full_parity(oracle_mod):
+    """Plain method, small workload: 128^3, brick 4, heightfield + 32 spheres, 640x480 camera (307,200 rays)."""
+    ops = svo.gen_scene(0, 128, 4, seed=0x5EED0001, spheres=32, octaves=2, base_freq=1.0 / 32,
+                        height_lo=0.0, height_hi=96.0)
+    o, p = both(oracle_mod, 128, 4, ops)
+    az = 0.7
+    eye = [64 + 200 * np.cos(0.5) * np.sin(az), 64 + 200 * np.sin(0.5), 64 + 200 * np.cos(0.5) * np.cos(az)]
+    origins, dirs = svo.gen_camera_rays(eye, [64, 64, 64], 60.0, 640, 480)
+    g = p.cast_host(origins, dirs)
+    c = o.cast(origins, dirs, threads=os.cpu_count() or 8)
+    assert_same_hits(g, c, counters=True, label="heightfield 640x480")
+    assert 0.2 < float(np.mean(g["status"] == 1)) < 0.99
+
+
+def test_device_pointer_cast_matches_host_cast(oracle_mod):
+    torch = pytest.importorskip("torch")
+    ops = svo.gen_scene(3, 64, 4, seed=5, occupancy=0.1, spheres=3, octaves=2, base_freq=1.0 / 16)
+    o, p = both(oracle_mod, 64, 4, ops)
+    origins, dirs = random_rays(np.random.default_rng(3), 64, 5000)
+    dev = torch.device("cuda:0")
+    cols = {k: torch.from_numpy(np.ascontiguousarray(a[:, i])).to(dev)
+            for a, names in ((origins, ("ox", "oy", "oz")), (dirs, ("dx", "dy", "dz"))) for i, k in enumerate(names)}
+    out = {k: torch.zeros(len(origins), dtype=getattr(torch, np.dtype(t).name), device=dev)
+           for k, t in svo.HIT_FIELDS.items()}
+    s = torch.cuda.current_stream().cuda_stream
+    p.cast({k: v.data_ptr() for k, v in cols.items()}, {k: v.data_ptr() for k, v in out.items()}, len(origins), s)
+    torch.cuda.synchronize()
+    g = {k: v.cpu().numpy() for k, v in out.items()}
+    assert_same_hits(g, o.cast(origins, dirs), counters=True, label="device pointers")
+    # only some outputs requested: the others are skipped, the requested ones are unchanged
+    part = {k: torch.zeros(len(origins), dtype=getattr(torch, np.dtype(svo.HIT_FIELDS[k]).name), device=dev)
+            for k in ("status", "albedo", "px")}
+    p.cast({k: v.data_ptr() for k, v in cols.items()}, {k: v.data_ptr() for k, v in part.items()}, len(origins), s)
+    torch.cuda.synchronize()
+    for k, v in part.items():
+        assert np.array_equal(v.cpu().numpy(), g[k])
+    p.cast({k: v.data_ptr() for k, v in cols.items()}, {}, 0, s)  # n == 0 is a no-op
+
+
+def test_in_place_sync_after_updates(oracle_mod):
+    ops = svo.gen_scene(0, 64, 4, seed=11, spheres=4, octaves=2, base_freq=1.0 / 16, height_lo=4.0, height_hi=30.0)
+    o, p = both(oracle_mod, 64, 4, ops)
+    rng = np.random.default_rng(5)
+    origins, dirs = random_rays(rng, 64, 3000)
+    assert_same_hits(p.cast_host(origins, dirs), o.cast(origins, dirs), label="before updates")
+    for step in range(3):
+        upd = np.zeros(200, dtype=ops.dtype)
+        for i in range(200):
+            x, y, z = rng.integers(0, 64, 3)
+            opk = int(rng.choice([0, 0, 3, 2, 4]))
+            sz = 1 if opk in (0, 3) else int(rng.choice([2, 4, 8]))
+            upd[i] = (x, y, z, opk, 3, sz, int(rng.choice([0xFF0000FF, 0x00FF00FF])), int(rng.integers(1, 9)))
+        o.apply_ops(upd)
+        p.apply_ops(upd)
+        p.sync()
+        assert_same_hits(p.cast_host(origins, dirs), o.cast(origins, dirs), counters=True, label="after sync %d" % step)
+    # a full re-upload of the same host state gives the same results as the in-place synced image
+    p.release_device()
+    p.upload()
+    assert_same_hits(p.cast_host(origins, dirs), o.cast(origins, dirs), counters=True, label="after re-upload")
+
+
+def test_not_uploaded_scene_is_rejected():
+    p = svo.Octree(16, 2)
+    p.insert((1, 1, 1), albedo=0xFF)
+    with pytest.raises(RuntimeError):
+        p.cast_host([[0, 0, -1]], [[0, 0, 1]])
+
+
+def test_batched_multi_scene_matches_single_scene_casts(oracle_mod):
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(9)
+    scenes, items, expected, keep = [], [], [], []
+    for j, (kind, size, dim, nrays) in enumerate([(3, 64, 2, 3000), (0, 128, 4, 5000), (3, 32, 8, 0),
+                                                  (1, 64, 8, 2000), (2, 128, 4, 4000), (3, 64, 1, 1500)]):
+        ops = svo.gen_scene(kind, size, dim, seed=200 + j, occupancy=0.1, spheres=2, octaves=2, base_freq=1.0 / 16,
+                            height_lo=2.0, height_hi=size * 0.3)
+        o, p = both(oracle_mod, size, dim, ops)
+        origins, dirs = random_rays(rng, size, nrays)
+        cols = {k: torch.from_numpy(np.ascontiguousarray(a[:, i]) if nrays else np.zeros(0, np.float32)).to(dev)
+                for a, names in ((origins, ("ox", "oy", "oz")), (dirs, ("dx", "dy", "dz")))
+                for i, k in enumerate(names)}
+        out = {k: torch.zeros(max(nrays, 1), dtype=getattr(torch, np.dtype(t).name), device=dev)
+               for k, t in svo.HIT_FIELDS.items()}
+        items.append((p, {k: v.data_ptr() for k, v in cols.items()}, nrays, {k: v.data_ptr() for k, v in out.items()}))
+        expected.append(o.cast(origins, dirs) if nrays else None)
+        scenes.append(p)
+        keep.append((cols, out))
+    ws = svo.BatchWorkspace()
+    for cfg in (svo.LaunchConfig(0, 0, 0, 0), svo.LaunchConfig(256, 32, 1, 0), svo.LaunchConfig(64, 512, 2, 0)):
+        for _, out in keep:
+            for v in out.values():
+                v.zero_()
+        ws.cast(items, cfg, torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        for j, ((_, out), exp) in enumerate(zip(keep, expected)):
+            if exp is None:
+                continue
+            n = len(exp["status"])
+            g = {k: v.cpu().numpy()[:n] for k, v in out.items()}
+            assert_same_hits(g, exp, counters=True, label="batch item %d cfg %d/%d" % (j, cfg.block, cfg.rays_per_chunk))
