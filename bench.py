@@ -179,6 +179,35 @@ def cpu_cast_rate(tree, origins, dirs, target_s, threads):
     return len(so) / dt, len(so), step, dt
 
 
+def batched_variants(svo, torch, scene, rp, hp, n, stream, args):
+    """The persistent work-queue kernel on the same batch: a short autotune sweep, then K timed steps."""
+    ws = svo.BatchWorkspace()
+    items = [(scene, rp, n, hp)]
+    s = stream.cuda_stream
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(cfg, reps):
+        ws.cast(items, cfg, s)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            ws.cast(items, cfg, s)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    sweep = []
+    for block in (64, 128, 256):
+        for chunk in (32, 64, 256):
+            cfg = svo.LaunchConfig(block, chunk, 0, 0)
+            sweep.append(((block, chunk), timed(cfg, 2)))
+    (block, chunk), _ = min(sweep, key=lambda t: t[1])
+    ms = timed(svo.LaunchConfig(block, chunk, 0, 0), args.steps)
+    return {"persistent_autotuned": {"value": round(n / (ms / 1e3) / 1e6, 3), "unit": "Mrays/s",
+                                     "ms_per_step": round(ms, 4), "block": block, "rays_per_chunk": chunk},
+            "sweep_ms": {"%dx%d" % k: round(v, 3) for k, v in sweep}}
+
+
 def run_reference(args, w):
     rank, _, world = dist_env()
     if rank != 0:
@@ -227,6 +256,7 @@ def main():
     ap.add_argument("--workload", default="terrain512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-variants", action="store_true", help="skip the persistent-kernel autotune sweep")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
@@ -301,6 +331,10 @@ def main():
     ms_step = ms / args.steps
     value = n * world / (ms_step / 1e3) / 1e6
 
+    variants = None
+    if not args.no_variants:
+        variants = batched_variants(svo, torch, scene, rp, hp, n, stream, args)
+
     # end to end through the host-buffer C-ABI call (pinned host memory)
     pin_cols = [torch.from_numpy(c).pin_memory() for c in cols_host]
     pin_out = {k: torch.empty(n, dtype=tmap[svo.HIT_FIELDS[k]]).pin_memory() for k in OUT_FIELDS}
@@ -340,6 +374,8 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": args.workload, "octree": "%d^3" % w["size"], "brick_dim": w["brick_dim"],
                        "rays_per_step": n, "hit_rate": round(hits / n, 4), "nodes": st["nodes"],
+                       "per_ray": {"node_visits": round(visits / n, 2), "child_reads": round(creads / n, 2),
+                                   "voxel_reads": round(vreads / n, 2)},
                        "parted_bricks": st["parted_bricks"], "voxels_inserted": int(len(ops)),
                        "l2": "inputs larger than L2 (rays %.0f MB + hits %.0f MB per step); the %.0f MB scene image "
                              "stays resident" % (n * 24 / 1e6, n * sum(OUT_BYTES.values()) / 1e6,
@@ -354,6 +390,7 @@ def main():
                     "d2h_bytes_per_step": n * sum(OUT_BYTES.values())},
             "gpu_launches": args.steps,
             "clocks": clk,
+            "variants": variants,
         }))
     if pg:
         pg.destroy_process_group()

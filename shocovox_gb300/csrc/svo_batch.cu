@@ -34,8 +34,10 @@ template <bool kCount>
 __global__ void batched_kernel(const BatchItemDev* __restrict__ items, uint32_t n_items, uint64_t total,
                                unsigned long long* __restrict__ counter, uint32_t chunk) {
   __shared__ uint64_t s_begin[kMaxSharedItems];
+  __shared__ SharedLuts L;
   const uint32_t staged = n_items < kMaxSharedItems ? n_items : kMaxSharedItems;
   for (uint32_t i = threadIdx.x; i < staged; i += blockDim.x) s_begin[i] = items[i].begin;
+  fill_shared_luts(L);
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31u;
   for (;;) {
@@ -61,7 +63,7 @@ __global__ void batched_kernel(const BatchItemDev* __restrict__ items, uint32_t 
       if (i >= it.n) continue;  // an empty item shares its begin with the next one
       const RaysView& r = it.rays;
       HitRecord h;
-      cast_ray<kCount>(it.scene, __ldg(r.ox + i), __ldg(r.oy + i), __ldg(r.oz + i), __ldg(r.dx + i),
+      cast_one<kCount>(it.scene, L, __ldg(r.ox + i), __ldg(r.oy + i), __ldg(r.oz + i), __ldg(r.dx + i),
                        __ldg(r.dy + i), __ldg(r.dz + i), h);
       write_hit(it.scene, it.hits, i, h);
       if (kCount) {

@@ -80,13 +80,16 @@ __device__ __forceinline__ float offx(uint32_t o) { return (float)(o & 1u); }
 __device__ __forceinline__ float offy(uint32_t o) { return (float)((o >> 2) & 1u); }
 __device__ __forceinline__ float offz(uint32_t o) { return (float)((o >> 1) & 1u); }
 
+// Every bounds size of the traversal is a power of two (the octree size is
+// brick_dim * 2^k and sizes only halve or double), so `inv` = 1 / s is exact
+// and x / s == x * inv bit for bit (both round the same exact value).
 struct Bounds {
-  float x, y, z, s;
+  float x, y, z, s, inv;
 };
 // Cube::child_bounds_for (src/spatial/mod.rs:32-39)
 __device__ __forceinline__ Bounds child_bounds(const Bounds& b, uint32_t o) {
-  const float h = b.s / 2.0f;
-  return Bounds{b.x + offx(o) * h, b.y + offy(o) * h, b.z + offz(o) * h, h};
+  const float h = b.s * 0.5f;
+  return Bounds{b.x + offx(o) * h, b.y + offy(o) * h, b.z + offz(o) * h, h, b.inv * 2.0f};
 }
 
 struct RayState {
@@ -96,14 +99,26 @@ struct RayState {
   float px, py, pz;     // current point
 };
 
-// dda_step_to_next_sibling (raytracing_on_cpu.rs:124-152)
+// dda_step_to_next_sibling (raytracing_on_cpu.rs:124-152).
+// kFast (direction without NaN, so signum is +-1): `size * max(g, 0) - g * e`
+// is `size - e` for g = +1 and `0 - (-e)` = e (up to the sign of a zero,
+// which the following abs() removes) for g = -1; the distances are >= 0 or
+// NaN, where fminf equals the NaN-ignoring Rust f32::min.
+template <bool kFast>
 __device__ __forceinline__ void dda_step(RayState& r, const Bounds& b, float& sx, float& sy, float& sz) {
   const float ex = r.px - b.x, ey = r.py - b.y, ez = r.pz - b.z;
-  const float nx = b.s * rmax(r.gx, 0.0f) - r.gx * ex;
-  const float ny = b.s * rmax(r.gy, 0.0f) - r.gy * ey;
-  const float nz = b.s * rmax(r.gz, 0.0f) - r.gz * ez;
+  float nx, ny, nz;
+  if (kFast) {
+    nx = r.gx > 0.0f ? b.s - ex : ex;
+    ny = r.gy > 0.0f ? b.s - ey : ey;
+    nz = r.gz > 0.0f ? b.s - ez : ez;
+  } else {
+    nx = b.s * rmax(r.gx, 0.0f) - r.gx * ex;
+    ny = b.s * rmax(r.gy, 0.0f) - r.gy * ey;
+    nz = b.s * rmax(r.gz, 0.0f) - r.gz * ez;
+  }
   const float ax = fabsf(nx * r.fx), ay = fabsf(ny * r.fy), az = fabsf(nz * r.fz);
-  const float m = rmin(rmin(ax, ay), az);
+  const float m = kFast ? fminf(fminf(ax, ay), az) : rmin(rmin(ax, ay), az);
   r.px = r.px + r.dx * m;
   r.py = r.py + r.dy * m;
   r.pz = r.pz + r.dz * m;
@@ -115,7 +130,7 @@ __device__ __forceinline__ void dda_step(RayState& r, const Bounds& b, float& sx
 // cube_impact_normal (src/spatial/raytracing/mod.rs:106-134)
 __device__ __forceinline__ void impact_normal(const Bounds& c, float px, float py, float pz, float& nx, float& ny,
                                               float& nz) {
-  const float h = c.s / 2.0f;
+  const float h = c.s * 0.5f;
   const float mx = (c.x + h) - px, my = (c.y + h) - py, mz = (c.z + h) - pz;
   const float m = rmax(rmax(fabsf(mx), fabsf(my)), fabsf(mz));
   const float vx = fabsf(mx) == m ? -mx : 0.0f;
@@ -137,7 +152,7 @@ enum : uint32_t { kKindNothing = 0, kKindInternal = 1, kKindLeaf = 2, kKindUnifo
 enum : uint32_t { kBkEmpty = 0, kBkSolid = 1, kBkParted = 2 };
 
 // Outcome of probe_brick: 0 miss, 1 hit, 2 work cap, 3 reference panic.
-template <bool kCount>
+template <bool kCount, bool kFast>
 __device__ __forceinline__ uint32_t probe_brick(const SceneView& s, RayState& r, uint32_t bk, uint32_t value,
                                                 const Bounds& bb, HitRecord& h, uint32_t& work) {
   if (bk == kBkEmpty) return 0;
@@ -153,13 +168,14 @@ __device__ __forceinline__ uint32_t probe_brick(const SceneView& s, RayState& r,
   // traverse_brick (raytracing_on_cpu.rs:156-252)
   const int D = (int)s.dim;
   const float Df = (float)s.dim;
-  int cx = min(max(as_i32((r.px - bb.x) * Df / bb.s), 0), D - 1);
-  int cy = min(max(as_i32((r.py - bb.y) * Df / bb.s), 0), D - 1);
-  int cz = min(max(as_i32((r.pz - bb.z) * Df / bb.s), 0), D - 1);
+  // x * D / size == (x * D) * (1 / size): size is a power of two
+  int cx = min(max(as_i32((r.px - bb.x) * Df * bb.inv), 0), D - 1);
+  int cy = min(max(as_i32((r.py - bb.y) * Df * bb.inv), 0), D - 1);
+  int cz = min(max(as_i32((r.pz - bb.z) * Df * bb.inv), 0), D - 1);
   int flat = cx + cy * D + cz * D * D;
   const int D3 = D * D * D;
-  const float unit = bb.s / Df;
-  Bounds cur{bb.x + (float)cx * unit, bb.y + (float)cy * unit, bb.z + (float)cz * unit, unit};
+  const float unit = bb.s * s.inv_dim;  // brick_bounds.size / brick_dim, exact
+  Bounds cur{bb.x + (float)cx * unit, bb.y + (float)cy * unit, bb.z + (float)cz * unit, unit, bb.inv * Df};
   const uint32_t* bits = s.vbits + (size_t)value * s.vwords;
   float sx = 0.0f, sy = 0.0f, sz = 0.0f;
   for (;;) {
@@ -169,8 +185,8 @@ __device__ __forceinline__ uint32_t probe_brick(const SceneView& s, RayState& r,
     if (kCount) h.vreads++;
     if (++work > kWorkCap) return 2;
     if ((__ldg(bits + (flat >> 5)) >> (flat & 31)) & 1u) {
-      const float hs = bb.s / Df;
-      const Bounds hb{bb.x + (float)cx * bb.s / Df, bb.y + (float)cy * bb.s / Df, bb.z + (float)cz * bb.s / Df, hs};
+      const Bounds hb{bb.x + (float)cx * bb.s * s.inv_dim, bb.y + (float)cy * bb.s * s.inv_dim,
+                      bb.z + (float)cz * bb.s * s.inv_dim, unit, bb.inv * Df};
       h.pix = __ldg(s.voxels + (size_t)value * (size_t)D3 + (size_t)flat);
       h.voxel = (uint32_t)flat;
       h.px = r.px;
@@ -179,7 +195,7 @@ __device__ __forceinline__ uint32_t probe_brick(const SceneView& s, RayState& r,
       impact_normal(hb, r.px, r.py, r.pz, h.nx, h.ny, h.nz);
       return 1;
     }
-    dda_step(r, cur, sx, sy, sz);
+    dda_step<kFast>(r, cur, sx, sy, sz);
     cur.x = cur.x + sx * unit;
     cur.y = cur.y + sy * unit;
     cur.z = cur.z + sz * unit;
@@ -200,9 +216,21 @@ __device__ __forceinline__ bool bitmap_index(float bx, float by, float bz, uint3
   return true;
 }
 
+// RAY_TO_NODE_OCCUPANCY_BITMASK_LUT and BITMAP_MASK_FOR_OCTANT_LUT staged in
+// shared memory by each block (computed with the arithmetic above).
+struct SharedLuts {
+  uint64_t ray_to_node[512];  // [pos * 8 + dir]
+  uint64_t octant[8];
+};
+__device__ __forceinline__ void fill_shared_luts(SharedLuts& L) {
+  for (uint32_t i = threadIdx.x; i < 512; i += blockDim.x) L.ray_to_node[i] = ray_to_node_mask(i >> 3, i & 7u);
+  if (threadIdx.x < 8) L.octant[threadIdx.x] = octant_mask(threadIdx.x);
+}
+
 // Octree::get_by_ray (raytracing_on_cpu.rs:316-565, MIP maps disabled)
-template <bool kCount>
-__device__ void cast_ray(const SceneView& s, float ox, float oy, float oz, float dx, float dy, float dz, HitRecord& h) {
+template <bool kCount, bool kFast>
+__device__ void cast_ray(const SceneView& s, const SharedLuts& L, float ox, float oy, float oz, float dx, float dy,
+                         float dz, HitRecord& h) {
   h.status = 0;
   h.octant = 0;
   h.node = 0;
@@ -225,8 +253,9 @@ __device__ void cast_ray(const SceneView& s, float ox, float oy, float oz, float
     r.fz = sqrtf((e * e + 1.0f) + f * f);
   }
   const uint32_t dir = hash_region(1.0f + dx, 1.0f + dy, 1.0f + dz, 1.0f);  // hash_direction
+  const uint64_t* rtn = L.ray_to_node + dir;
   const float S = s.size;
-  Bounds cb{0.0f, 0.0f, 0.0f, S};
+  Bounds cb{0.0f, 0.0f, 0.0f, S, s.inv_size};
   uint32_t target;
   {  // Cube::intersect_ray (src/spatial/raytracing/mod.rs:32-61) on the root bounds
     const float t1 = (0.0f - ox) / dx, t2 = ((0.0f + S) - ox) / dx;
@@ -239,12 +268,12 @@ __device__ void cast_ray(const SceneView& s, float ox, float oy, float oz, float
     r.px = ox + dx * t;
     r.py = oy + dy * t;
     r.pz = oz + dz * t;
-    target = hash_region(r.px - 0.0f, r.py - 0.0f, r.pz - 0.0f, S / 2.0f);
+    target = hash_region(r.px - 0.0f, r.py - 0.0f, r.pz - 0.0f, S * 0.5f);
   }
   uint32_t work = 0;
   while (target != kOob) {
     uint32_t cur = 0;
-    cb = Bounds{0.0f, 0.0f, 0.0f, S};
+    cb = Bounds{0.0f, 0.0f, 0.0f, S, s.inv_size};
     // NodeStack<u32, 4> (:20-82) as a shift register: the newest entry in s0
     uint32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0, count = 1;
     while (count > 0) {
@@ -261,7 +290,7 @@ __device__ void cast_ray(const SceneView& s, float ox, float oy, float oz, float
       bool backtrack = kind == kKindUniform;
       if (target != kOob) {
         if (kind == kKindUniform) {
-          const uint32_t rc = probe_brick<kCount>(s, r, (meta >> 8) & 3u, __ldg(&nd->slot[0]), cb, h, work);
+          const uint32_t rc = probe_brick<kCount, kFast>(s, r, (meta >> 8) & 3u, __ldg(&nd->slot[0]), cb, h, work);
           if (rc) {
             h.status = rc;
             h.node = cur;
@@ -270,8 +299,8 @@ __device__ void cast_ray(const SceneView& s, float ox, float oy, float oz, float
           }
           backtrack = true;
         } else if (kind == kKindLeaf) {
-          const uint32_t rc = probe_brick<kCount>(s, r, (meta >> (8 + 2 * target)) & 3u, __ldg(&nd->slot[target]),
-                                                  child_bounds(cb, target), h, work);
+          const uint32_t rc = probe_brick<kCount, kFast>(s, r, (meta >> (8 + 2 * target)) & 3u,
+                                                         __ldg(&nd->slot[target]), child_bounds(cb, target), h, work);
           if (rc) {
             h.status = rc;
             h.node = cur;
@@ -280,15 +309,15 @@ __device__ void cast_ray(const SceneView& s, float ox, float oy, float oz, float
           }
         }
       }
-      float bx = rclamp((r.px - cb.x) * 4.0f / cb.s, kTol, 4.0f - kTol);
-      float by = rclamp((r.py - cb.y) * 4.0f / cb.s, kTol, 4.0f - kTol);
-      float bz = rclamp((r.pz - cb.z) * 4.0f / cb.s, kTol, 4.0f - kTol);
+      float bx = rclamp((r.px - cb.x) * 4.0f * cb.inv, kTol, 4.0f - kTol);
+      float by = rclamp((r.py - cb.y) * 4.0f * cb.inv, kTol, 4.0f - kTol);
+      float bz = rclamp((r.pz - cb.z) * 4.0f * cb.inv, kTol, 4.0f - kTol);
       uint32_t flat;
       if (!bitmap_index(bx, by, bz, flat)) {
         h.status = 3;
         return;
       }
-      if (backtrack || target == kOob || occ == 0 || (occ & ray_to_node_mask(flat, dir)) == 0) {
+      if (backtrack || target == kOob || occ == 0 || (occ & rtn[flat * 8u]) == 0) {
         // POP (:445-473)
         s0 = s1;
         s1 = s2;
@@ -296,24 +325,26 @@ __device__ void cast_ray(const SceneView& s, float ox, float oy, float oz, float
         --count;
         if (count > 0) {
           cur = s0;
-          const float h2 = cb.s / 2.0f, s2x = cb.s * 2.0f;
-          const float pmx = cb.x - fmodf(cb.x, s2x), pmy = cb.y - fmodf(cb.y, s2x), pmz = cb.z - fmodf(cb.z, s2x);
+          // min - fmod(min, 2s): bounds minima are non-negative multiples of s and 2s is a power of
+          // two, so fmod(x, 2s) == x - floor(x / 2s) * 2s exactly and the parent minimum is floor(x / 2s) * 2s
+          const float h2 = cb.s * 0.5f, s2x = cb.s * 2.0f, i2x = cb.inv * 0.5f;
+          const float pmx = floorf(cb.x * i2x) * s2x, pmy = floorf(cb.y * i2x) * s2x, pmz = floorf(cb.z * i2x) * s2x;
           const uint32_t ho = hash_region((cb.x + h2) - pmx, (cb.y + h2) - pmy, (cb.z + h2) - pmz, cb.s);
           float sx, sy, sz;
-          dda_step(r, cb, sx, sy, sz);
+          dda_step<kFast>(r, cb, sx, sy, sz);
           target = step_octant(ho, sx, sy, sz);
-          cb = Bounds{pmx, pmy, pmz, cb.s * 2.0f};
+          cb = Bounds{pmx, pmy, pmz, s2x, i2x};
         }
         continue;
       }
       Bounds tb = child_bounds(cb, target);
       uint32_t ck = kind == kKindInternal ? __ldg(&nd->slot[target]) : kInvalidChild;
       if (kCount) h.creads++;
-      if (ck != kInvalidChild && (occ & octant_mask(target)) != 0) {
+      if (ck != kInvalidChild && (occ & L.octant[target]) != 0) {
         // PUSH (:484-492)
         cur = ck;
         cb = tb;
-        target = hash_region(r.px - tb.x, r.py - tb.y, r.pz - tb.z, tb.s / 2.0f);
+        target = hash_region(r.px - tb.x, r.py - tb.y, r.pz - tb.z, tb.s * 0.5f);
         s3 = s2;
         s2 = s1;
         s1 = s0;
@@ -327,23 +358,22 @@ __device__ void cast_ray(const SceneView& s, float ox, float oy, float oz, float
             return;
           }
           float sx, sy, sz;
-          dda_step(r, tb, sx, sy, sz);
+          dda_step<kFast>(r, tb, sx, sy, sz);
           target = step_octant(target, sx, sy, sz);
           if (target != kOob) {
             tb = child_bounds(cb, target);
             ck = kind == kKindInternal ? __ldg(&nd->slot[target]) : kInvalidChild;
             if (kCount) h.creads++;
-            bx = bx + sx * 4.0f / cb.s;
-            by = by + sy * 4.0f / cb.s;
-            bz = bz + sz * 4.0f / cb.s;
+            bx = bx + sx * 4.0f * cb.inv;
+            by = by + sy * 4.0f * cb.inv;
+            bz = bz + sz * 4.0f * cb.inv;
             if (!bitmap_index(bx, by, bz, flat)) {
               h.status = 3;
               return;
             }
           }
           if (target == kOob) break;
-          if (ck != kInvalidChild && (occ & octant_mask(target)) != 0 && (ray_to_node_mask(flat, dir) & occ) != 0)
-            break;
+          if (ck != kInvalidChild && (occ & L.octant[target]) != 0 && (rtn[flat * 8u] & occ) != 0) break;
           if (kind == kKindLeaf && ((meta >> (8 + 2 * target)) & 3u) != kBkEmpty) break;
         }
       }
@@ -353,9 +383,27 @@ __device__ void cast_ray(const SceneView& s, float ox, float oy, float oz, float
     r.py = r.py + dy * 0.1f;
     r.pz = r.pz + dz * 0.1f;
     target = (r.px < S && r.py < S && r.pz < S && r.px > 0.0f && r.py > 0.0f && r.pz > 0.0f)
-                 ? hash_region(r.px, r.py, r.pz, S / 2.0f)
+                 ? hash_region(r.px, r.py, r.pz, S * 0.5f)
                  : kOob;
   }
+}
+
+// Rays whose direction holds a NaN take the literal form, out of line so that
+// it does not add to the fast path's register allocation.
+template <bool kCount>
+__device__ __noinline__ void cast_ray_literal(const SceneView& s, const SharedLuts& L, float ox, float oy, float oz,
+                                              float dx, float dy, float dz, HitRecord& h) {
+  cast_ray<kCount, false>(s, L, ox, oy, oz, dx, dy, dz, h);
+}
+
+// One ray: the exact fast form when the direction holds no NaN, the literal form otherwise.
+template <bool kCount>
+__device__ __forceinline__ void cast_one(const SceneView& s, const SharedLuts& L, float ox, float oy, float oz,
+                                         float dx, float dy, float dz, HitRecord& h) {
+  if (!isnan(dx) && !isnan(dy) && !isnan(dz))
+    cast_ray<kCount, true>(s, L, ox, oy, oz, dx, dy, dz, h);
+  else
+    cast_ray_literal<kCount>(s, L, ox, oy, oz, dx, dy, dz, h);
 }
 
 struct HitsView {

@@ -17,10 +17,13 @@ namespace svo {
 
 template <bool kCount>
 __global__ void __launch_bounds__(128) cast_kernel(SceneView s, RaysView rays, HitsView out, uint64_t n) {
+  __shared__ SharedLuts L;
+  fill_shared_luts(L);
+  __syncthreads();
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   HitRecord h;
-  cast_ray<kCount>(s, __ldg(rays.ox + i), __ldg(rays.oy + i), __ldg(rays.oz + i), __ldg(rays.dx + i),
+  cast_one<kCount>(s, L, __ldg(rays.ox + i), __ldg(rays.oy + i), __ldg(rays.oz + i), __ldg(rays.dx + i),
                    __ldg(rays.dy + i), __ldg(rays.dz + i), h);
   write_hit(s, out, i, h);
   if (kCount) {
@@ -46,6 +49,8 @@ SceneView scene_view(const svo_scene* sc) {
   const uint32_t len = sc->tree.arena.len();
   v.vwords = len >= 32 ? len / 32 : 1;
   v.size = (float)sc->tree.size;
+  v.inv_size = 1.0f / v.size;
+  v.inv_dim = 1.0f / (float)v.dim;
   return v;
 }
 

@@ -35,6 +35,8 @@ struct SceneView {
   uint32_t dim;     // brick dimension D
   uint32_t vwords;  // max(1, D^3 / 32)
   float size;       // octree size
+  float inv_size;   // 1 / size (exact: a power of two)
+  float inv_dim;    // 1 / D (exact: a power of two)
 };
 
 struct DeviceImage {
