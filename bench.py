@@ -295,6 +295,8 @@ def main():
     hp = {k: v.data_ptr() for k, v in outs.items()}
     s = stream.cuda_stream
 
+    clocks = ClockSampler(local_rank)
+    clocks.start()  # samples from the warm-up on, so that short timed regions still get samples
     for _ in range(args.warmup):
         scene.cast(rp, hp, n, s)
     torch.cuda.synchronize()
@@ -309,8 +311,6 @@ def main():
     alg_bytes = 12 * visits + 4 * creads + 4 * vreads + 8 * hits
     del cnt
 
-    clocks = ClockSampler(local_rank)
-    clocks.start()
     if pg:
         pg.barrier()
     torch.cuda.synchronize()
@@ -323,7 +323,6 @@ def main():
     ms = e0.elapsed_time(e1)
     if pg:
         pg.barrier()
-    clk = clocks.stop()
     if pg:
         t = torch.tensor([ms], dtype=torch.float64)
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
@@ -334,6 +333,7 @@ def main():
     variants = None
     if not args.no_variants:
         variants = batched_variants(svo, torch, scene, rp, hp, n, stream, args)
+    clk = clocks.stop()
 
     # end to end through the host-buffer C-ABI call (pinned host memory)
     pin_cols = [torch.from_numpy(c).pin_memory() for c in cols_host]

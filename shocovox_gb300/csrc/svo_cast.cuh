@@ -309,14 +309,14 @@ __device__ void cast_ray(const SceneView& s, const SharedLuts& L, float ox, floa
           }
         }
       }
-      float bx = rclamp((r.px - cb.x) * 4.0f * cb.inv, kTol, 4.0f - kTol);
-      float by = rclamp((r.py - cb.y) * 4.0f * cb.inv, kTol, 4.0f - kTol);
-      float bz = rclamp((r.pz - cb.z) * 4.0f * cb.inv, kTol, 4.0f - kTol);
-      uint32_t flat;
-      if (!bitmap_index(bx, by, bz, flat)) {
-        h.status = 3;
-        return;
-      }
+      // bitmap position of the point in the node; floor(clamp(v, 1e-5, 4 - 1e-5)) as usize equals
+      // min(trunc_to_u32(v), 3) for every v including NaN and +-inf, so the clamped values
+      // themselves are only formed when ADVANCE needs them
+      const float rx = (r.px - cb.x) * 4.0f * cb.inv;
+      const float ry = (r.py - cb.y) * 4.0f * cb.inv;
+      const float rz = (r.pz - cb.z) * 4.0f * cb.inv;
+      uint32_t flat = min(__float2uint_rz(rx), 3u) + 4u * min(__float2uint_rz(ry), 3u) +
+                      16u * min(__float2uint_rz(rz), 3u);
       if (backtrack || target == kOob || occ == 0 || (occ & rtn[flat * 8u]) == 0) {
         // POP (:445-473)
         s0 = s1;
@@ -352,6 +352,9 @@ __device__ void cast_ray(const SceneView& s, const SharedLuts& L, float ox, floa
         count = count < 4 ? count + 1 : 4;
       } else {
         // ADVANCE (:494-544)
+        float bx = rclamp(rx, kTol, 4.0f - kTol);
+        float by = rclamp(ry, kTol, 4.0f - kTol);
+        float bz = rclamp(rz, kTol, 4.0f - kTol);
         for (;;) {
           if (++work > kWorkCap) {
             h.status = 2;
