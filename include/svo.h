@@ -203,6 +203,11 @@ svo_status svo_gen_sphere_rays(const float center[3], float radius, uint64_t n, 
  * BITMAP_MASK_FOR_OCTANT_LUT[8] (src/spatial/lut.rs) for comparison with the
  * reference constants.  Allocates a few bytes of device memory. */
 svo_status svo_selftest_luts(uint64_t* ray_to_node, uint32_t* octant_step, uint64_t* octant_masks);
+/* Selects the form of the cast kernels for casts launched afterwards (process-wide):
+ * 0 (default) the fast form for rays without NaN in the direction and the literal
+ * restatement otherwise; 1 the literal restatement for every ray.  Both give the
+ * same results; mode 1 exists so tests can check that. */
+svo_status svo_set_cast_mode(int32_t mode);
 
 #ifdef __cplusplus
 }

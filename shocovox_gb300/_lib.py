@@ -85,6 +85,7 @@ SIGNATURES = {
     "svo_gen_camera_rays": (_I32, [_P(_F), _P(_F), _F, _U32, _U32, _VP, _VP, _VP, _VP, _VP, _VP]),
     "svo_gen_sphere_rays": (_I32, [_P(_F), _F, _U64, _U64, _VP, _VP, _VP, _VP, _VP, _VP]),
     "svo_selftest_luts": (_I32, [_P(_U64), _P(_U32), _P(_U64)]),
+    "svo_set_cast_mode": (_I32, [_I32]),
 }
 
 

@@ -391,6 +391,256 @@ __device__ void cast_ray(const SceneView& s, const SharedLuts& L, float ox, floa
   }
 }
 
+// ---------------------------------------------------------------------------
+// Fast form of the same cast for directions without NaN (signum is +-1 on every
+// axis).  It performs the reference's operations on every value it keeps; only
+// the bookkeeping around them is cheaper, each step justified where it appears:
+//  * a DDA step returns the 3-bit set of axes that advance (octant bit layout:
+//    x = 1, z = 2, y = 4) instead of a float step vector whose entries are
+//    +-1 or 0, so step_octant's LUT becomes `o ^ move`, out of bounds when a
+//    moved axis is already on the far side in the ray's direction;
+//  * `x + step * k` with step in {+-1, +0} is `moved ? x + sign * k : x`;
+//  * POP's parent octant: a node minimum is either the parent minimum or the
+//    parent minimum + size, so hash_region(center - parent_min, size) tests
+//    `min != parent_min` per axis.
+struct FastRay {
+  float dx, dy, dz;  // direction
+  float fx, fy, fz;  // dda scale factors
+  float px, py, pz;  // current point
+  uint32_t pos;      // axes with a positive direction, octant bit layout
+};
+
+// dda_step_to_next_sibling (raytracing_on_cpu.rs:124-152), returning the moved axes
+__device__ __forceinline__ uint32_t dda_move(FastRay& r, float bx, float by, float bz, float bs) {
+  const float ex = r.px - bx, ey = r.py - by, ez = r.pz - bz;
+  const float nx = (r.pos & 1u) ? bs - ex : ex;
+  const float ny = (r.pos & 4u) ? bs - ey : ey;
+  const float nz = (r.pos & 2u) ? bs - ez : ez;
+  const float ax = fabsf(nx * r.fx), ay = fabsf(ny * r.fy), az = fabsf(nz * r.fz);
+  const float m = fminf(fminf(ax, ay), az);
+  r.px = r.px + r.dx * m;
+  r.py = r.py + r.dy * m;
+  r.pz = r.pz + r.dz * m;
+  return (m == ax ? 1u : 0u) | (m == az ? 2u : 0u) | (m == ay ? 4u : 0u);
+}
+
+// step_octant for a step along the moved axes in the ray's direction
+__device__ __forceinline__ uint32_t step_fast(uint32_t o, uint32_t move, uint32_t pos) {
+  return (((o ^ pos) ^ 7u) & move) ? kOob : (o ^ move);
+}
+
+// probe_brick / traverse_brick (raytracing_on_cpu.rs:156-312), fast form
+template <bool kCount>
+__device__ __forceinline__ uint32_t probe_brick_fast(const SceneView& s, FastRay& r, uint32_t bk, uint32_t value,
+                                                     const Bounds& bb, HitRecord& h, uint32_t& work) {
+  if (bk == kBkEmpty) return 0;
+  if (bk == kBkSolid) {
+    h.pix = value;
+    h.voxel = 0xFFFFFFFFu;
+    h.px = r.px;
+    h.py = r.py;
+    h.pz = r.pz;
+    impact_normal(bb, r.px, r.py, r.pz, h.nx, h.ny, h.nz);
+    return 1;
+  }
+  const int D = (int)s.dim;
+  const float Df = (float)s.dim;
+  int cx = min(max(as_i32((r.px - bb.x) * Df * bb.inv), 0), D - 1);
+  int cy = min(max(as_i32((r.py - bb.y) * Df * bb.inv), 0), D - 1);
+  int cz = min(max(as_i32((r.pz - bb.z) * Df * bb.inv), 0), D - 1);
+  int flat = cx + cy * D + cz * D * D;
+  const int D3 = D * D * D;
+  const float unit = bb.s * s.inv_dim;
+  float ux = bb.x + (float)cx * unit, uy = bb.y + (float)cy * unit, uz = bb.z + (float)cz * unit;
+  const float gux = (r.pos & 1u) ? unit : -unit, guy = (r.pos & 4u) ? unit : -unit, guz = (r.pos & 2u) ? unit : -unit;
+  const int ix = (r.pos & 1u) ? 1 : -1, iy = (r.pos & 4u) ? 1 : -1, iz = (r.pos & 2u) ? 1 : -1;
+  const int fdx = ix, fdy = iy * D, fdz = iz * D * D;
+  const uint32_t* bits = s.vbits + (size_t)value * s.vwords;
+  uint32_t move = 0;
+  for (;;) {
+    if ((unsigned)cx >= (unsigned)D || (unsigned)cy >= (unsigned)D || (unsigned)cz >= (unsigned)D) return 0;
+    flat += ((move & 1u) ? fdx : 0) + ((move & 4u) ? fdy : 0) + ((move & 2u) ? fdz : 0);
+    if ((unsigned)flat >= (unsigned)D3) return 3;
+    if (kCount) h.vreads++;
+    if (++work > kWorkCap) return 2;
+    if ((__ldg(bits + (flat >> 5)) >> (flat & 31)) & 1u) {
+      const Bounds hb{bb.x + (float)cx * bb.s * s.inv_dim, bb.y + (float)cy * bb.s * s.inv_dim,
+                      bb.z + (float)cz * bb.s * s.inv_dim, unit, bb.inv * Df};
+      h.pix = __ldg(s.voxels + (size_t)value * (size_t)D3 + (size_t)flat);
+      h.voxel = (uint32_t)flat;
+      h.px = r.px;
+      h.py = r.py;
+      h.pz = r.pz;
+      impact_normal(hb, r.px, r.py, r.pz, h.nx, h.ny, h.nz);
+      return 1;
+    }
+    move = dda_move(r, ux, uy, uz, unit);
+    if (move & 1u) {
+      ux = ux + gux;
+      cx += ix;
+    }
+    if (move & 4u) {
+      uy = uy + guy;
+      cy += iy;
+    }
+    if (move & 2u) {
+      uz = uz + guz;
+      cz += iz;
+    }
+  }
+}
+
+template <bool kCount>
+__device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox, float oy, float oz, float dx,
+                              float dy, float dz, HitRecord& h) {
+  h.status = 0;
+  h.octant = 0;
+  h.node = 0;
+  h.voxel = 0xFFFFFFFFu;
+  h.pix = 0;
+  h.px = h.py = h.pz = h.nx = h.ny = h.nz = 0.0f;
+  if (kCount) h.visits = h.creads = h.vreads = 0;
+
+  FastRay r;
+  r.dx = dx;
+  r.dy = dy;
+  r.dz = dz;
+  {  // get_dda_scale_factors (:99-112); powf(q, 2.) == q * q
+    const float a = dz / dx, b = dy / dx, c = dx / dy, d = dz / dy, e = dx / dz, f = dy / dz;
+    r.fx = sqrtf((1.0f + a * a) + b * b);
+    r.fy = sqrtf((c * c + 1.0f) + d * d);
+    r.fz = sqrtf((e * e + 1.0f) + f * f);
+  }
+  // signum(d) > 0 <=> d > 0 or d == +0
+  r.pos = (rsignum(dx) > 0.0f ? 1u : 0u) | (rsignum(dz) > 0.0f ? 2u : 0u) | (rsignum(dy) > 0.0f ? 4u : 0u);
+  const float g4x = (r.pos & 1u) ? 4.0f : -4.0f, g4y = (r.pos & 4u) ? 4.0f : -4.0f, g4z = (r.pos & 2u) ? 4.0f : -4.0f;
+  const uint32_t dir = hash_region(1.0f + dx, 1.0f + dy, 1.0f + dz, 1.0f);
+  const uint64_t* rtn = L.ray_to_node + dir;
+  const float S = s.size;
+  Bounds cb{0.0f, 0.0f, 0.0f, S, s.inv_size};
+  uint32_t target;
+  {
+    const float t1 = (0.0f - ox) / dx, t2 = ((0.0f + S) - ox) / dx;
+    const float t3 = (0.0f - oy) / dy, t4 = ((0.0f + S) - oy) / dy;
+    const float t5 = (0.0f - oz) / dz, t6 = ((0.0f + S) - oz) / dz;
+    const float tmin = rmax(rmax(rmin(t1, t2), rmin(t3, t4)), rmin(t5, t6));
+    const float tmax = rmin(rmin(rmax(t1, t2), rmax(t3, t4)), rmax(t5, t6));
+    if (tmax < 0.0f || tmin > tmax) return;
+    const float t = tmin < 0.0f ? 0.0f : tmin;
+    r.px = ox + dx * t;
+    r.py = oy + dy * t;
+    r.pz = oz + dz * t;
+    target = hash_region(r.px - 0.0f, r.py - 0.0f, r.pz - 0.0f, S * 0.5f);
+  }
+  uint32_t work = 0;
+  while (target != kOob) {
+    uint32_t cur = 0;
+    cb = Bounds{0.0f, 0.0f, 0.0f, S, s.inv_size};
+    uint32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0, count = 1;
+    while (count > 0) {
+      if (++work > kWorkCap) {
+        h.status = 2;
+        return;
+      }
+      if (kCount) h.visits++;
+      const DevNode* nd = s.nodes + cur;
+      const uint4 head = __ldg(reinterpret_cast<const uint4*>(nd));
+      const uint64_t occ = ((uint64_t)head.y << 32) | head.x;
+      const uint32_t meta = head.z;
+      const uint32_t kind = meta & 3u;
+      const bool uniform = kind == kKindUniform;
+      const bool backtrack = uniform;  // a UniformLeaf is always left after its probe
+      if (target != kOob && (uniform || kind == kKindLeaf)) {
+        // probe the UniformLeaf's brick over the node bounds, or the Leaf's brick under target_octant
+        const uint32_t slot = uniform ? 0u : target;
+        const uint32_t bk = (meta >> (8 + 2 * slot)) & 3u;
+        if (bk != kBkEmpty) {
+          const uint32_t rc = probe_brick_fast<kCount>(s, r, bk, __ldg(&nd->slot[slot]),
+                                                       uniform ? cb : child_bounds(cb, target), h, work);
+          if (rc) {
+            h.status = rc;
+            h.node = cur;
+            h.octant = slot;
+            return;
+          }
+        }
+      }
+      const float rx = (r.px - cb.x) * 4.0f * cb.inv;
+      const float ry = (r.py - cb.y) * 4.0f * cb.inv;
+      const float rz = (r.pz - cb.z) * 4.0f * cb.inv;
+      uint32_t flat = min(__float2uint_rz(rx), 3u) + 4u * min(__float2uint_rz(ry), 3u) +
+                      16u * min(__float2uint_rz(rz), 3u);
+      if (backtrack || target == kOob || occ == 0 || (occ & rtn[flat * 8u]) == 0) {
+        // POP
+        s0 = s1;
+        s1 = s2;
+        s2 = s3;
+        --count;
+        if (count > 0) {
+          cur = s0;
+          const float s2x = cb.s * 2.0f, i2x = cb.inv * 0.5f;
+          const float pmx = floorf(cb.x * i2x) * s2x, pmy = floorf(cb.y * i2x) * s2x, pmz = floorf(cb.z * i2x) * s2x;
+          const uint32_t ho = (cb.x != pmx ? 1u : 0u) | (cb.z != pmz ? 2u : 0u) | (cb.y != pmy ? 4u : 0u);
+          const uint32_t move = dda_move(r, cb.x, cb.y, cb.z, cb.s);
+          target = step_fast(ho, move, r.pos);
+          cb = Bounds{pmx, pmy, pmz, s2x, i2x};
+        }
+        continue;
+      }
+      Bounds tb = child_bounds(cb, target);
+      uint32_t ck = kind == kKindInternal ? __ldg(&nd->slot[target]) : kInvalidChild;
+      if (kCount) h.creads++;
+      if (ck != kInvalidChild && (occ & L.octant[target]) != 0) {
+        // PUSH
+        cur = ck;
+        cb = tb;
+        target = hash_region(r.px - tb.x, r.py - tb.y, r.pz - tb.z, tb.s * 0.5f);
+        s3 = s2;
+        s2 = s1;
+        s1 = s0;
+        s0 = ck;
+        count = count < 4 ? count + 1 : 4;
+      } else {
+        // ADVANCE
+        float bx = rclamp(rx, kTol, 4.0f - kTol);
+        float by = rclamp(ry, kTol, 4.0f - kTol);
+        float bz = rclamp(rz, kTol, 4.0f - kTol);
+        const float dbx = g4x * cb.inv, dby = g4y * cb.inv, dbz = g4z * cb.inv;
+        for (;;) {
+          if (++work > kWorkCap) {
+            h.status = 2;
+            return;
+          }
+          const uint32_t move = dda_move(r, tb.x, tb.y, tb.z, tb.s);
+          target = step_fast(target, move, r.pos);
+          if (target == kOob) break;
+          tb = child_bounds(cb, target);
+          ck = kind == kKindInternal ? __ldg(&nd->slot[target]) : kInvalidChild;
+          if (kCount) h.creads++;
+          if (move & 1u) bx = bx + dbx;
+          if (move & 4u) by = by + dby;
+          if (move & 2u) bz = bz + dbz;
+          // floor(bp) as usize: the reference panics at 4 and above
+          const uint32_t ux = __float2uint_rz(bx), uy = __float2uint_rz(by), uz = __float2uint_rz(bz);
+          if (ux >= 4u || uy >= 4u || uz >= 4u) {
+            h.status = 3;
+            return;
+          }
+          flat = ux + 4u * uy + 16u * uz;
+          if (ck != kInvalidChild && (occ & L.octant[target]) != 0 && (rtn[flat * 8u] & occ) != 0) break;
+          if (kind == kKindLeaf && ((meta >> (8 + 2 * target)) & 3u) != kBkEmpty) break;
+        }
+      }
+    }
+    r.px = r.px + dx * 0.1f;
+    r.py = r.py + dy * 0.1f;
+    r.pz = r.pz + dz * 0.1f;
+    target = (r.px < S && r.py < S && r.pz < S && r.px > 0.0f && r.py > 0.0f && r.pz > 0.0f)
+                 ? hash_region(r.px, r.py, r.pz, S * 0.5f)
+                 : kOob;
+  }
+}
+
 // Rays whose direction holds a NaN take the literal form, out of line so that
 // it does not add to the fast path's register allocation.
 template <bool kCount>
@@ -403,8 +653,8 @@ __device__ __noinline__ void cast_ray_literal(const SceneView& s, const SharedLu
 template <bool kCount>
 __device__ __forceinline__ void cast_one(const SceneView& s, const SharedLuts& L, float ox, float oy, float oz,
                                          float dx, float dy, float dz, HitRecord& h) {
-  if (!isnan(dx) && !isnan(dy) && !isnan(dz))
-    cast_ray<kCount, true>(s, L, ox, oy, oz, dx, dy, dz, h);
+  if (!s.literal && !isnan(dx) && !isnan(dy) && !isnan(dz))
+    cast_ray_fast<kCount>(s, L, ox, oy, oz, dx, dy, dz, h);
   else
     cast_ray_literal<kCount>(s, L, ox, oy, oz, dx, dy, dz, h);
 }

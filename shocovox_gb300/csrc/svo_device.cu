@@ -33,6 +33,8 @@ __global__ void __launch_bounds__(128) cast_kernel(SceneView s, RaysView rays, H
   }
 }
 
+int g_cast_mode = 0;
+
 // ------------------------------------------------------------------ device image
 SceneView scene_view(const svo_scene* sc) {
   const DeviceImage& d = sc->dev;
@@ -51,6 +53,7 @@ SceneView scene_view(const svo_scene* sc) {
   v.size = (float)sc->tree.size;
   v.inv_size = 1.0f / v.size;
   v.inv_dim = 1.0f / (float)v.dim;
+  v.literal = g_cast_mode == 1 ? 1u : 0u;
   return v;
 }
 
@@ -355,6 +358,12 @@ svo_status svo_cast_host(svo_scene* sc, const svo_rays* rays, uint64_t n, const 
     if (host_fields[f])
       SVO_CUDA_TRY(cudaMemcpyAsync(host_fields[f], dev_fields[f], kFieldBytes[f] * n, cudaMemcpyDeviceToHost, st));
   SVO_CUDA_TRY(cudaStreamSynchronize(st));
+  return SVO_OK;
+}
+
+svo_status svo_set_cast_mode(int32_t mode) {
+  if (mode != 0 && mode != 1) return fail(SVO_ERR_ARGUMENT, "svo_set_cast_mode: mode must be 0 or 1");
+  g_cast_mode = mode;
   return SVO_OK;
 }
 

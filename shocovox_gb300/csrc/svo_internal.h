@@ -37,7 +37,11 @@ struct SceneView {
   float size;       // octree size
   float inv_size;   // 1 / size (exact: a power of two)
   float inv_dim;    // 1 / D (exact: a power of two)
+  uint32_t literal; // 1: every ray takes the literal form of the cast (diagnostics)
 };
+
+// Cast form selected by svo_set_cast_mode (0 automatic, 1 literal only).
+extern int g_cast_mode;
 
 struct DeviceImage {
   DevNode* nodes = nullptr;

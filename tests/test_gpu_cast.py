@@ -122,6 +122,13 @@ def random_rays(rng, size, n, inside_frac=0.3):
         if not np.any(v):
             v = np.array([0, -1, 0], dtype=np.float32)
         d[i] = normalized(v.astype(np.float32))
+    # inputs outside the reference's debug preconditions still get its release-mode results:
+    # NaN, infinite, zero, signed-zero and subnormal direction components
+    special = np.array([[np.nan, 0.5, 0.5], [0.0, 0.0, 0.0], [np.inf, 1.0, 0.0], [-0.0, -1.0, 0.0],
+                        [1e-40, -1.0, 1e-40], [0.0, -0.0, 1.0], [-np.inf, -np.inf, 0.25], [np.nan] * 3],
+                       dtype=np.float32)
+    k = min(len(special), n // 10)
+    d[:k] = special[:k]
     return o, d
 
 
@@ -135,6 +142,24 @@ def test_generated_scenes_random_rays(oracle_mod, kind, size, dim):
     origins, dirs = random_rays(rng, size, 4000)
     assert_same_hits(p.cast_host(origins, dirs), o.cast(origins, dirs, threads=8), counters=True,
                      label="kind%d %d/%d" % (kind, size, dim))
+
+
+@pytest.mark.parametrize("kind,size,dim", [(0, 64, 2), (1, 128, 8), (2, 128, 4), (3, 64, 16)])
+def test_literal_form_matches_oracle(oracle_mod, kind, size, dim):
+    """Mode 1 sends every ray through the literal restatement; it must match the oracle as the fast form does."""
+    ops = svo.gen_scene(kind, size, dim, seed=301 + size + dim, occupancy=0.12, spheres=4, octaves=2,
+                        base_freq=1.0 / 16, height_lo=2.0, height_hi=size * 0.4, cave_threshold=0.55)
+    o, p = both(oracle_mod, size, dim, ops)
+    origins, dirs = random_rays(np.random.default_rng(kind + size), size, 3000)
+    expect = o.cast(origins, dirs, threads=8)
+    assert svo.lib().svo_set_cast_mode(1) == 0
+    try:
+        literal = p.cast_host(origins, dirs)
+    finally:
+        assert svo.lib().svo_set_cast_mode(0) == 0
+    assert_same_hits(literal, expect, counters=True, label="literal form")
+    assert_same_hits(p.cast_host(origins, dirs), expect, counters=True, label="fast form")
+    assert svo.lib().svo_set_cast_mode(7) != 0
 
 
 def test_small_heightfield_camera_full_parity(oracle_mod):
