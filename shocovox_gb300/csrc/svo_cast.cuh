@@ -693,6 +693,7 @@ __device__ __forceinline__ void write_hit(const SceneView& s, const HitsView& o,
     h.px = h.py = h.pz = h.nx = h.ny = h.nz = 0.0f;
     kind = albedo = user = 0;
   }
+  if (h.status >= 2) h.visits = h.creads = h.vreads = 0;  // no defined counts past a cap or panic
   if (o.status) o.status[i] = (uint8_t)h.status;
   if (o.octant) o.octant[i] = (uint8_t)h.octant;
   if (o.kind) o.kind[i] = (uint8_t)kind;
