@@ -32,8 +32,11 @@ def assert_same_hits(gpu, cpu, counters=False, label=""):
             label, f, len(bad), n, bad[0], gpu[f][bad[0]], cpu[f][bad[0]])
     for f in FLOAT_FIELDS:
         g, c = gpu[f].astype(np.float64), cpu[f].astype(np.float64)
-        both_nan = np.isnan(g) & np.isnan(c)  # e.g. a NaN-direction ray that the reference reports as a hit
-        d = np.where(both_nan, 0.0, np.abs(g - c))
+        # identical values (also infinities) and NaN on both sides (e.g. a NaN-direction ray that the
+        # reference reports as a hit) agree; everything else must be within TOL
+        same = (g == c) | (np.isnan(g) & np.isnan(c))
+        with np.errstate(invalid="ignore"):
+            d = np.where(same, 0.0, np.abs(g - c))
         bad = np.nonzero(~(d <= TOL))[0]
         assert len(bad) == 0, "%s: %s differs on %d rays, first %d: gpu %r cpu %r" % (
             label, f, len(bad), bad[0], g[bad[0]], c[bad[0]])
