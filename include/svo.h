@@ -175,6 +175,20 @@ void svo_batch_workspace_destroy(svo_batch_workspace* ws);
 svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items, uint32_t n_items,
                             const svo_launch_config* cfg, void* stream);
 
+/* Allocation-free variant of svo_cast_batched for callers that cannot allocate
+ * device memory when they cast (a fixed memory budget handed over at start-up,
+ * or a frame loop where a cudaMalloc would synchronise the device).  No
+ * counterpart in the reference.  The item table and work counter live in one
+ * scratch array compiled into the library (36,096 bytes, reserved on every GPU
+ * that loads the library until the process exits), so at most 128 items are
+ * accepted per call; more return SVO_ERR_ARGUMENT.  The first call on a device
+ * looks up the array's device address (make it before any stream capture).
+ * Calls that overlap on the GPU share the array and race: issue them on one
+ * stream, or wait for one before starting the next.  Allocates nothing and
+ * calls no allocating CUDA or library routine. */
+svo_status svo_cast_batched_noalloc(const svo_batch_item* items, uint32_t n_items, const svo_launch_config* cfg,
+                                    void* stream);
+
 /* ---- synthetic workloads (seeded, deterministic on x86_64 and aarch64) ---- */
 typedef struct {
   uint32_t kind;      /* 0 heightfield+spheres, 1 terrain+caves, 2 sparse+uniform blocks, 3 noise+spheres */

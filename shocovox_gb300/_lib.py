@@ -81,6 +81,7 @@ SIGNATURES = {
     "svo_batch_workspace_create": (_I32, [_P(_VP)]),
     "svo_batch_workspace_destroy": (None, [_VP]),
     "svo_cast_batched": (_I32, [_VP, _P(BatchItem), _U32, _P(LaunchConfig), _VP]),
+    "svo_cast_batched_noalloc": (_I32, [_P(BatchItem), _U32, _P(LaunchConfig), _VP]),
     "svo_gen_scene": (_I32, [_P(SceneRecipe), _VP, _U64, _P(_U64)]),
     "svo_gen_camera_rays": (_I32, [_P(_F), _P(_F), _F, _U32, _U32, _VP, _VP, _VP, _VP, _VP, _VP]),
     "svo_gen_sphere_rays": (_I32, [_P(_F), _F, _U64, _U64, _VP, _VP, _VP, _VP, _VP, _VP]),

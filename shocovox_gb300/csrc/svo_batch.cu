@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -206,6 +207,114 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
     batched_kernel<true><<<(unsigned)grid, block, 0, st>>>(ws->d_items, n_items, total, ws->d_counter, chunk);
   else
     batched_kernel<false><<<(unsigned)grid, block, 0, st>>>(ws->d_items, n_items, total, ws->d_counter, chunk);
+  SVO_CUDA_TRY(cudaGetLastError());
+  return SVO_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free batched cast.
+//
+// Some callers of this library cannot allocate device memory at the moment they
+// cast: an engine that hands the library a fixed memory budget and forbids
+// allocation after start-up, or code running inside a frame loop or a graph of
+// its own where a cudaMalloc would synchronise the device.  For them the item
+// table and the work counter of the batched cast live in the fixed scratch
+// array below instead of an svo_batch_workspace.  The array is reserved on
+// every GPU that loads the library, for as long as the process lives.
+constexpr uint32_t kNoAllocMaxItems = 128;  // items per call
+constexpr size_t kNoAllocTableBytes = kNoAllocMaxItems * sizeof(svo::BatchItemDev);
+constexpr size_t kNoAllocCounterOffset = (kNoAllocTableBytes + 255) / 256 * 256;
+constexpr size_t kNoAllocBytes = kNoAllocCounterOffset + 256;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+int g_noalloc_sms[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on the current device, looked up once per device.
+svo_status noalloc_scratch(void** out, int* sms) {
+  int dev = 0;
+  SVO_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: device ordinal too large");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* ptr = nullptr;
+    SVO_CUDA_TRY(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+    int n = 0;
+    SVO_CUDA_TRY(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+    g_noalloc_ptr[dev] = ptr;
+    g_noalloc_sms[dev] = n;
+  }
+  *out = g_noalloc_ptr[dev];
+  *sms = g_noalloc_sms[dev];
+  return SVO_OK;
+}
+}  // namespace
+
+extern "C" {
+
+svo_status svo_cast_batched_noalloc(const svo_batch_item* items, uint32_t n_items, const svo_launch_config* cfg,
+                                    void* stream) {
+  if (!items && n_items) return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: NULL items");
+  if (n_items > kNoAllocMaxItems)
+    return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: " + std::to_string(n_items) + " items exceed the maximum of " +
+                                      std::to_string(kNoAllocMaxItems) + " per call");
+  if (n_items == 0) return SVO_OK;
+  void* scratch = nullptr;
+  int sms = 0;
+  svo_status rc = noalloc_scratch(&scratch, &sms);
+  if (rc != SVO_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  BatchItemDev table[kNoAllocMaxItems];
+  uint64_t total = 0;
+  bool count = false;
+  for (uint32_t i = 0; i < n_items; ++i) {
+    const svo_batch_item& it = items[i];
+    if (!it.scene) return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: NULL scene");
+    if (!it.scene->dev.valid) return fail(SVO_ERR_NOT_UPLOADED, "svo_cast_batched_noalloc: scene not uploaded");
+    if (it.n && (!it.rays.ox || !it.rays.oy || !it.rays.oz || !it.rays.dx || !it.rays.dy || !it.rays.dz))
+      return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: NULL ray array");
+    BatchItemDev& d = table[i];
+    d.scene = scene_view(it.scene);
+    d.rays = RaysView{it.rays.ox, it.rays.oy, it.rays.oz, it.rays.dx, it.rays.dy, it.rays.dz};
+    d.hits = hits_view_of(it.hits);
+    d.begin = total;
+    d.n = it.n;
+    total += it.n;
+    count |= it.hits.node_visits || it.hits.child_reads || it.hits.voxel_reads;
+  }
+  if (total == 0) return SVO_OK;
+  const uint32_t block = (cfg && cfg->block) ? cfg->block : 128;
+  const uint32_t chunk = (cfg && cfg->rays_per_chunk) ? cfg->rays_per_chunk : 64;
+  if (block % 32 != 0 || block > 1024 || chunk == 0)
+    return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: bad launch config");
+  int per_sm = (cfg && cfg->blocks_per_sm) ? (int)cfg->blocks_per_sm : 0;
+  if (per_sm == 0) {
+    if (count)
+      SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_kernel<true>, block, 0));
+    else
+      SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_kernel<false>, block, 0));
+    per_sm = std::max(per_sm, 1);
+  }
+  const uint64_t warps_needed = (total + chunk - 1) / chunk;
+  uint64_t grid = (uint64_t)sms * (uint64_t)per_sm;
+  grid = std::min<uint64_t>(grid, (warps_needed * 32 + block - 1) / block);
+  grid = std::max<uint64_t>(grid, 1);
+  BatchItemDev* d_items = static_cast<BatchItemDev*>(scratch);
+  unsigned long long* d_counter =
+      reinterpret_cast<unsigned long long*>(static_cast<unsigned char*>(scratch) + kNoAllocCounterOffset);
+  // the table is copied from this stack frame: a pageable source is staged before cudaMemcpyAsync returns
+  SVO_CUDA_TRY(cudaMemcpyAsync(d_items, table, n_items * sizeof(BatchItemDev), cudaMemcpyHostToDevice, st));
+  // the counter keeps the previous call's final value: reset it for this launch
+  SVO_CUDA_TRY(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st));
+  if (count)
+    batched_kernel<true><<<(unsigned)grid, block, 0, st>>>(d_items, n_items, total, d_counter, chunk);
+  else
+    batched_kernel<false><<<(unsigned)grid, block, 0, st>>>(d_items, n_items, total, d_counter, chunk);
   SVO_CUDA_TRY(cudaGetLastError());
   return SVO_OK;
 }
