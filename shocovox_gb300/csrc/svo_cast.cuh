@@ -537,6 +537,7 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
     uint32_t cur = 0;
     cb = Bounds{0.0f, 0.0f, 0.0f, S, s.inv_size};
     uint32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0, count = 1;
+    uint32_t oct = 0;  // octant of each stack entry in its parent, newest in the low 3 bits
     while (count > 0) {
       if (++work > kWorkCap) {
         h.status = 2;
@@ -571,19 +572,23 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
       uint32_t flat = min(__float2uint_rz(rx), 3u) + 4u * min(__float2uint_rz(ry), 3u) +
                       16u * min(__float2uint_rz(rz), 3u);
       if (backtrack || target == kOob || occ == 0 || (occ & rtn[flat * 8u]) == 0) {
-        // POP
+        // POP.  The popped node was pushed as child `ho` of the new top, so its bounds are
+        // child_bounds_for(parent, ho): the reference's parent minimum min - fmod(min, 2 size) is
+        // min - offset(ho) * size and hash_region(center - parent_min, size) is ho (both exact).
+        const uint32_t ho = oct & 7u;
         s0 = s1;
         s1 = s2;
         s2 = s3;
+        oct >>= 3;
         --count;
         if (count > 0) {
           cur = s0;
-          const float s2x = cb.s * 2.0f, i2x = cb.inv * 0.5f;
-          const float pmx = floorf(cb.x * i2x) * s2x, pmy = floorf(cb.y * i2x) * s2x, pmz = floorf(cb.z * i2x) * s2x;
-          const uint32_t ho = (cb.x != pmx ? 1u : 0u) | (cb.z != pmz ? 2u : 0u) | (cb.y != pmy ? 4u : 0u);
+          const float pmx = (ho & 1u) ? cb.x - cb.s : cb.x;
+          const float pmy = (ho & 4u) ? cb.y - cb.s : cb.y;
+          const float pmz = (ho & 2u) ? cb.z - cb.s : cb.z;
           const uint32_t move = dda_move(r, cb.x, cb.y, cb.z, cb.s);
           target = step_fast(ho, move, r.pos);
-          cb = Bounds{pmx, pmy, pmz, s2x, i2x};
+          cb = Bounds{pmx, pmy, pmz, cb.s * 2.0f, cb.inv * 0.5f};
         }
         continue;
       }
@@ -591,7 +596,8 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
       uint32_t ck = kind == kKindInternal ? __ldg(&nd->slot[target]) : kInvalidChild;
       if (kCount) h.creads++;
       if (ck != kInvalidChild && (occ & L.octant[target]) != 0) {
-        // PUSH
+        // PUSH (the child's octant in its parent rides along: 3 bits per stack entry)
+        oct = ((oct << 3) | target) & 0xFFFu;
         cur = ck;
         cb = tb;
         target = hash_region(r.px - tb.x, r.py - tb.y, r.pz - tb.z, tb.s * 0.5f);

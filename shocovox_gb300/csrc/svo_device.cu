@@ -16,7 +16,7 @@
 namespace svo {
 
 template <bool kCount>
-__global__ void __launch_bounds__(128) cast_kernel(SceneView s, RaysView rays, HitsView out, uint64_t n) {
+__global__ void __launch_bounds__(128, 7) cast_kernel(SceneView s, RaysView rays, HitsView out, uint64_t n) {
   __shared__ SharedLuts L;
   fill_shared_luts(L);
   __syncthreads();
