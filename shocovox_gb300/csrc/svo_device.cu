@@ -259,6 +259,107 @@ svo_status launch_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const sv
   return SVO_OK;
 }
 
+// Host-buffer cast, pipelined: the batch is cut into chunks cast on three
+// streams in turn, so chunk i+1's host->device copy and chunk i-1's
+// device->host copy overlap chunk i's kernel (with pinned host memory; with
+// pageable memory the copies still run, only without overlap).
+constexpr int kPipeStreams = 3;
+constexpr size_t kFieldBytes[17] = {1, 1, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4};
+
+struct HostPipeline {
+  cudaStream_t st[kPipeStreams] = {};
+  cudaEvent_t ready = nullptr;                 // caller's stream reached the call
+  cudaEvent_t done[kPipeStreams] = {};         // a pipeline stream finished its chunks
+  char* buf[kPipeStreams] = {};
+  size_t buf_bytes = 0;
+};
+
+void destroy_pipeline(DeviceImage& d) {
+  HostPipeline* p = static_cast<HostPipeline*>(d.ws);
+  if (!p) return;
+  for (int i = 0; i < kPipeStreams; ++i) {
+    if (p->st[i]) cudaStreamSynchronize(p->st[i]);
+    cudaFree(p->buf[i]);
+    if (p->st[i]) cudaStreamDestroy(p->st[i]);
+    if (p->done[i]) cudaEventDestroy(p->done[i]);
+  }
+  if (p->ready) cudaEventDestroy(p->ready);
+  delete p;
+  d.ws = nullptr;
+  d.ws_bytes = 0;
+}
+
+svo_status cast_host_pipelined(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_hits* hits,
+                               cudaStream_t caller) {
+  DeviceImage& d = sc->dev;
+  void* const* host_fields = reinterpret_cast<void* const*>(hits);
+  size_t per_ray = 24;
+  for (int f = 0; f < 17; ++f)
+    if (host_fields[f]) per_ray += kFieldBytes[f];
+  const uint64_t chunk = std::min<uint64_t>(n, std::max<uint64_t>(262144, ((n / 6 + 255) / 256) * 256));
+  const size_t need = (size_t)chunk * per_ray + 32 * 256;
+  HostPipeline* p = static_cast<HostPipeline*>(d.ws);
+  if (!p) {
+    p = new HostPipeline();
+    d.ws = p;
+    for (int i = 0; i < kPipeStreams; ++i) {
+      SVO_CUDA_TRY(cudaStreamCreateWithFlags(&p->st[i], cudaStreamNonBlocking));
+      SVO_CUDA_TRY(cudaEventCreateWithFlags(&p->done[i], cudaEventDisableTiming));
+    }
+    SVO_CUDA_TRY(cudaEventCreateWithFlags(&p->ready, cudaEventDisableTiming));
+  }
+  if (need > p->buf_bytes) {
+    for (int i = 0; i < kPipeStreams; ++i) {
+      SVO_CUDA_TRY(cudaStreamSynchronize(p->st[i]));
+      cudaFree(p->buf[i]);
+      p->buf[i] = nullptr;
+    }
+    p->buf_bytes = 0;
+    for (int i = 0; i < kPipeStreams; ++i) SVO_CUDA_TRY(cudaMalloc(&p->buf[i], need));
+    p->buf_bytes = need;
+    d.ws_bytes = need * kPipeStreams;
+  }
+  // the pipeline streams start after the work already queued on the caller's stream
+  SVO_CUDA_TRY(cudaEventRecord(p->ready, caller));
+  for (int i = 0; i < kPipeStreams; ++i) SVO_CUDA_TRY(cudaStreamWaitEvent(p->st[i], p->ready, 0));
+  const float* hr[6] = {rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz};
+  uint64_t c = 0;
+  for (uint64_t off = 0; off < n; off += chunk, ++c) {
+    const uint64_t m = std::min<uint64_t>(chunk, n - off);
+    const int k = (int)(c % kPipeStreams);
+    cudaStream_t st = p->st[k];
+    char* base = p->buf[k];
+    size_t o = 0;
+    float* dr[6];
+    for (int a = 0; a < 6; ++a) {
+      dr[a] = reinterpret_cast<float*>(base + o);
+      o += ((chunk * 4 + 255) / 256) * 256;
+      SVO_CUDA_TRY(cudaMemcpyAsync(dr[a], hr[a] + off, m * 4, cudaMemcpyHostToDevice, st));
+    }
+    svo_hits dh;
+    std::memset(&dh, 0, sizeof(dh));
+    void** dev_fields = reinterpret_cast<void**>(&dh);
+    for (int f = 0; f < 17; ++f)
+      if (host_fields[f]) {
+        dev_fields[f] = base + o;
+        o += ((kFieldBytes[f] * chunk + 255) / 256) * 256;
+      }
+    svo_rays drays{dr[0], dr[1], dr[2], dr[3], dr[4], dr[5]};
+    svo_status rc = launch_cast(sc, &drays, m, &dh, st);
+    if (rc != SVO_OK) return rc;
+    for (int f = 0; f < 17; ++f)
+      if (host_fields[f])
+        SVO_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(host_fields[f]) + off * kFieldBytes[f], dev_fields[f],
+                                     kFieldBytes[f] * m, cudaMemcpyDeviceToHost, st));
+  }
+  for (int i = 0; i < kPipeStreams; ++i) {
+    SVO_CUDA_TRY(cudaEventRecord(p->done[i], p->st[i]));
+    SVO_CUDA_TRY(cudaStreamWaitEvent(caller, p->done[i], 0));
+  }
+  SVO_CUDA_TRY(cudaStreamSynchronize(caller));
+  return SVO_OK;
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ LUT self-test kernel
@@ -293,10 +394,8 @@ svo_status svo_scene_sync(svo_scene* sc, void* stream) {
 
 svo_status svo_scene_release_device(svo_scene* sc) {
   if (!sc) return fail(SVO_ERR_ARGUMENT, "NULL scene");
+  destroy_pipeline(sc->dev);
   free_device(sc->dev);
-  cudaFree(sc->dev.ws);
-  sc->dev.ws = nullptr;
-  sc->dev.ws_bytes = 0;
   std::fill(sc->tree.node_dirty.begin(), sc->tree.node_dirty.end(), 1);
   std::fill(sc->tree.arena.dirty().begin(), sc->tree.arena.dirty().end(), 1);
   return SVO_OK;
@@ -304,8 +403,8 @@ svo_status svo_scene_release_device(svo_scene* sc) {
 
 void svo_scene_destroy(svo_scene* sc) {
   if (!sc) return;
+  destroy_pipeline(sc->dev);
   free_device(sc->dev);
-  cudaFree(sc->dev.ws);
   delete sc;
 }
 
@@ -321,44 +420,9 @@ svo_status svo_cast_host(svo_scene* sc, const svo_rays* rays, uint64_t n, const 
   if (!sc || !rays || !hits) return fail(SVO_ERR_ARGUMENT, "svo_cast_host: NULL argument");
   if (!sc->dev.valid) return fail(SVO_ERR_NOT_UPLOADED, "svo_cast_host: scene has no device image");
   if (n == 0) return SVO_OK;
-  cudaStream_t st = (cudaStream_t)stream;
-  // workspace layout: 6 ray arrays then one slot per hit field (bytes per element below)
-  static const size_t kFieldBytes[17] = {1, 1, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4};
-  void* const* host_fields = reinterpret_cast<void* const*>(hits);
-  size_t need = 6 * n * 4;
-  for (int f = 0; f < 17; ++f)
-    if (host_fields[f]) need += ((kFieldBytes[f] * n + 255) / 256) * 256;
-  if (need > sc->dev.ws_bytes) {
-    cudaFree(sc->dev.ws);
-    sc->dev.ws = nullptr;
-    sc->dev.ws_bytes = 0;
-    SVO_CUDA_TRY(cudaMalloc(&sc->dev.ws, need));
-    sc->dev.ws_bytes = need;
-  }
-  char* base = static_cast<char*>(sc->dev.ws);
-  float* dr[6];
-  const float* hr[6] = {rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz};
-  for (int a = 0; a < 6; ++a) {
-    dr[a] = reinterpret_cast<float*>(base + (size_t)a * n * 4);
-    SVO_CUDA_TRY(cudaMemcpyAsync(dr[a], hr[a], n * 4, cudaMemcpyHostToDevice, st));
-  }
-  svo_hits dh;
-  std::memset(&dh, 0, sizeof(dh));
-  void** dev_fields = reinterpret_cast<void**>(&dh);
-  size_t off = 6 * n * 4;
-  for (int f = 0; f < 17; ++f)
-    if (host_fields[f]) {
-      dev_fields[f] = base + off;
-      off += ((kFieldBytes[f] * n + 255) / 256) * 256;
-    }
-  svo_rays drays{dr[0], dr[1], dr[2], dr[3], dr[4], dr[5]};
-  svo_status rc = launch_cast(sc, &drays, n, &dh, st);
-  if (rc != SVO_OK) return rc;
-  for (int f = 0; f < 17; ++f)
-    if (host_fields[f])
-      SVO_CUDA_TRY(cudaMemcpyAsync(host_fields[f], dev_fields[f], kFieldBytes[f] * n, cudaMemcpyDeviceToHost, st));
-  SVO_CUDA_TRY(cudaStreamSynchronize(st));
-  return SVO_OK;
+  if (!rays->ox || !rays->oy || !rays->oz || !rays->dx || !rays->dy || !rays->dz)
+    return fail(SVO_ERR_ARGUMENT, "svo_cast_host: NULL ray array");
+  return cast_host_pipelined(sc, rays, n, hits, (cudaStream_t)stream);
 }
 
 svo_status svo_set_cast_mode(int32_t mode) {
