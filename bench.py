@@ -38,7 +38,10 @@ WORKLOADS = {
                            height_lo=0.0, height_hi=96.0, cave_threshold=0.55, rays=("orbit", 1, 640, 480, 60.0)),
     "incoherent1024": dict(kind=2, size=1024, brick_dim=8, seed=0x5EED0003, occupancy=0.05,
                            rays=("sphere", 1 << 22)),
+    "multiscene64": dict(multi=64, seed=0x5EED0004),
+    "served16": dict(served=16, seed=0x5EED0005, rate=2000.0, requests=600, budget_gb=60.0),
 }
+RESOLUTIONS = [(320, 240), (640, 480), (1280, 720), (1920, 1080), (3840, 2160)]
 OUT_FIELDS = ("status", "entry_kind", "albedo", "user", "px", "py", "pz", "nx", "ny", "nz")
 OUT_BYTES = {"status": 1, "entry_kind": 1, "albedo": 4, "user": 4, "px": 4, "py": 4, "pz": 4, "nx": 4, "ny": 4,
              "nz": 4}
@@ -208,6 +211,285 @@ def batched_variants(svo, torch, scene, rp, hp, n, stream, args):
             "sweep_ms": {"%dx%d" % k: round(v, 3) for k, v in sweep}}
 
 
+def multiscene_specs(w):
+    """64 scenes: size from {64..512}^3, brick dim from {2,4,8}, occupancy 2-20%, noise + spheres,
+    a log-uniform 1K-1M ray batch each (half camera rays, half random directions)."""
+    rng = np.random.default_rng(w["seed"])
+    specs = []
+    for i in range(w["multi"]):
+        size = int(rng.choice([64, 128, 256, 512]))
+        dim = int(rng.choice([2, 4, 8]))
+        occ = float(rng.uniform(0.02, 0.20))
+        nrays = int(np.exp(rng.uniform(np.log(1e3), np.log(1e6))))
+        specs.append(dict(kind=3, size=size, brick_dim=dim, seed=w["seed"] + 17 * i, occupancy=occ, spheres=8,
+                          octaves=2, base_freq=1.0 / 32, nrays=nrays, eye_angle=float(rng.uniform(0, 2 * np.pi))))
+    return specs
+
+
+def multiscene_rays(svo, sp):
+    S = float(sp["size"])
+    n = sp["nrays"]
+    ncam = n // 2
+    w_ = max(1, int(np.ceil(np.sqrt(ncam * 16 / 9))))
+    h_ = max(1, int(np.ceil(ncam / w_)))
+    a = sp["eye_angle"]
+    eye = [S / 2 + 1.6 * S * np.cos(a), 1.2 * S, S / 2 + 1.6 * S * np.sin(a)]
+    o1, d1 = svo.gen_camera_rays(eye, [S / 2, S / 3, S / 2], 60.0, w_, h_)
+    o2, d2 = svo.gen_sphere_rays([S / 2] * 3, S * np.sqrt(3.0) / 2, n - ncam, sp["seed"])
+    return np.concatenate([o1[:ncam], o2]), np.concatenate([d1[:ncam], d2])
+
+
+def run_multiscene(args, w):
+    """Batched multi-scene cast: serial plain dispatch vs one persistent launch vs that launch in a CUDA graph."""
+    import concurrent.futures as cf
+    import torch
+    import shocovox_gb300 as svo
+    from shocovox_gb300 import autotune
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    specs = multiscene_specs(w)
+    t0 = time.perf_counter()
+
+    def build(sp):
+        ops = svo.gen_scene(sp["kind"], sp["size"], sp["brick_dim"], sp["seed"], occupancy=sp["occupancy"],
+                            spheres=sp["spheres"], octaves=sp["octaves"], base_freq=sp["base_freq"])
+        t = svo.Octree(sp["size"], sp["brick_dim"])
+        t.apply_ops(ops)
+        return t, len(ops)
+
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        built = list(ex.map(build, specs))
+    build_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream(dev)
+    s = stream.cuda_stream
+    tmap = {np.uint8: torch.uint8, np.uint32: torch.int32, np.float32: torch.float32}
+    scenes, items, host_rays, outs = [], [], [], []
+    for sp, (t, _) in zip(specs, built):
+        t.upload(s)
+        o, d = multiscene_rays(svo, sp)
+        cols = [np.ascontiguousarray(o[:, i]) for i in range(3)] + [np.ascontiguousarray(d[:, i]) for i in range(3)]
+        rays = {k: torch.from_numpy(c).to(dev) for k, c in zip(("ox", "oy", "oz", "dx", "dy", "dz"), cols)}
+        out = {k: torch.empty(len(o), dtype=tmap[svo.HIT_FIELDS[k]], device=dev) for k in OUT_FIELDS}
+        scenes.append(t)
+        host_rays.append((o, d, cols))
+        outs.append(out)
+        items.append((t, {k: v.data_ptr() for k, v in rays.items()}, len(o),
+                      {k: v.data_ptr() for k, v in out.items()}, rays))
+    total = sum(it[2] for it in items)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def serial():
+        for (t, rp, n, hp, _) in items:
+            t.cast(rp, hp, n, s)
+
+    ws = svo.BatchWorkspace()
+    bitems = [(t, rp, n, hp) for (t, rp, n, hp, _) in items]
+    cfg, tune_info = autotune.tune(ws, bitems, torch.cuda.get_device_name(0),
+                                   lambda c: timed(lambda: ws.cast(bitems, c, s), 2))
+
+    def batched():
+        ws.cast(bitems, cfg, s)
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    for _ in range(args.warmup):
+        serial()
+        batched()
+    torch.cuda.synchronize()
+    serial_ms = timed(serial, args.steps)
+    ref_out = [{k: v.clone() for k, v in out.items()} for out in outs]
+    batched_ms = timed(batched, args.steps)
+    same = all(torch.equal(a[k], b[k]) for a, b in zip(ref_out, outs) for k in OUT_FIELDS)
+    # one persistent launch captured in a CUDA graph (workspace already sized, blocks per SM fixed)
+    if cfg.blocks_per_sm == 0:
+        per_sm = {64: 16, 128: 7, 256: 3}.get(cfg.block, 2)
+        gcfg = svo.LaunchConfig(cfg.block, cfg.rays_per_chunk, per_sm, 0)
+    else:
+        gcfg = cfg
+    gstream = torch.cuda.Stream(dev)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(gstream):
+        ws.cast(bitems, gcfg, gstream.cuda_stream)
+        torch.cuda.synchronize()
+        with torch.cuda.graph(graph, stream=gstream):
+            ws.cast(bitems, gcfg, gstream.cuda_stream)
+    torch.cuda.synchronize()
+    graph_ms = timed(graph.replay, args.steps)
+    clk = clocks.stop()
+
+    # algorithmic bytes of the batch, from the instrumented batched cast
+    cnt = [{k: torch.zeros(n, dtype=torch.int32, device=dev) for k in ("status", "node_visits", "child_reads",
+                                                                        "voxel_reads")} for (_, _, n, _, _) in items]
+    citems = [(t, rp, n, {k: v.data_ptr() for k, v in c.items()}) for (t, rp, n, _, _), c in zip(items, cnt)]
+    ws.cast(citems, cfg, s)
+    torch.cuda.synchronize()
+    sums = {k: sum(int(c[k].to(torch.int64).sum()) for c in cnt) for k in ("node_visits", "child_reads", "voxel_reads")}
+    hits = sum(int(((c["status"] & 0xFF) == 1).sum()) for c in cnt)
+    alg = 12 * sums["node_visits"] + 4 * sums["child_reads"] + 4 * sums["voxel_reads"] + 8 * hits
+
+    # end to end: host rays in, one batched launch, host hits out (pinned buffers, copies in the timed region)
+    pin_in = [[torch.from_numpy(c).pin_memory() for c in cols] for (_, _, cols) in host_rays]
+    pin_out = [{k: torch.empty(len(o), dtype=tmap[svo.HIT_FIELDS[k]]).pin_memory() for k in OUT_FIELDS}
+               for (o, _, _) in host_rays]
+
+    def e2e():
+        for (_, _, _, _, rays), pins in zip(items, pin_in):
+            for k, p in zip(("ox", "oy", "oz", "dx", "dy", "dz"), pins):
+                rays[k].copy_(p, non_blocking=True)
+        ws.cast(bitems, cfg, s)
+        for out, po in zip(outs, pin_out):
+            for k in OUT_FIELDS:
+                po[k].copy_(out[k], non_blocking=True)
+
+    e2e()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t1) / args.steps
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle
+        # a bounded sample: the 8 cheapest scenes to rebuild on the CPU, 20k rays each at most
+        order = sorted(range(len(specs)), key=lambda i: built[i][1])[:8]
+        rays_done, secs = 0, 0.0
+        threads = os.cpu_count() or 1
+        for i in order:
+            sp = specs[i]
+            ops = svo.gen_scene(sp["kind"], sp["size"], sp["brick_dim"], sp["seed"], occupancy=sp["occupancy"],
+                                spheres=sp["spheres"], octaves=sp["octaves"], base_freq=sp["base_freq"])
+            ot = oracle.Tree(sp["size"], sp["brick_dim"])
+            ot.apply_ops(ops)
+            o, d, _ = host_rays[i]
+            step = max(1, len(o) // 20000)
+            tt = time.perf_counter()
+            ot.cast(o[::step], d[::step], threads=threads)
+            secs += time.perf_counter() - tt
+            rays_done += len(o[::step])
+        cpu = {"value": round(rays_done / secs / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": "%d rays over the 8 smallest of the 64 scenes" % rays_done}
+
+    peak, peak_src = measured_peak()
+    print(json.dumps({
+        "metric": "Mrays/s", "value": round(total / (graph_ms / 1e3) / 1e6, 3), "unit": "Mrays/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(graph_ms, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "multiscene64", "scenes": len(specs), "rays_per_step": total,
+                   "sizes": sorted({sp["size"] for sp in specs}), "brick_dims": sorted({sp["brick_dim"] for sp in specs}),
+                   "voxels_inserted": int(sum(b[1] for b in built)), "build_s": round(build_s, 1),
+                   "l2": "rays %.0f MB + hits %.0f MB per step (larger than L2)" % (total * 24 / 1e6, total * 34 / 1e6),
+                   "timed": "one persistent batched launch replayed from a CUDA graph",
+                   "serial_plain": {"value": round(total / (serial_ms / 1e3) / 1e6, 3), "ms_per_step": round(serial_ms, 4),
+                                    "launches_per_step": len(items)},
+                   "batched": {"value": round(total / (batched_ms / 1e3) / 1e6, 3), "ms_per_step": round(batched_ms, 4)},
+                   "batched_equals_serial": bool(same),
+                   "autotune": {"block": cfg.block, "rays_per_chunk": cfg.rays_per_chunk, "cached": tune_info["cached"],
+                                "sweep_ms": tune_info.get("sweep_ms")}},
+        "roofline": {"bound": "hbm", "achieved": round(alg / (graph_ms / 1e3) / 1e9, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(alg / (graph_ms / 1e3) / 1e9 / peak, 4), "traffic": None, "peak_source": peak_src,
+                     "alg_bytes_per_launch": alg, "alg_bytes_per_ray": round(alg / total, 2)},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(total / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": total * 24,
+                "d2h_bytes_per_step": total * sum(OUT_BYTES.values())},
+        "gpu_launches": args.steps,
+        "clocks": clk,
+    }))
+
+
+def run_served(args, w):
+    """Served load: Poisson camera requests over 16 resident scenes, continuous batching vs serial dispatch."""
+    import torch
+    import shocovox_gb300 as svo
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(w["seed"])
+    sizes = [int(rng.choice([256, 512, 1024, 2048])) for _ in range(w["served"])]
+    t0 = time.perf_counter()
+    scenes = []
+    for i, S in enumerate(sizes):
+        ops = svo.gen_scene(4, S, 8, w["seed"] + 31 * i, occupancy=float(rng.uniform(0.01, 0.05)))
+        t = svo.Octree(S, 8)
+        t.apply_ops(ops)
+        scenes.append(t)
+    build_s = time.perf_counter() - t0
+    n_req = w["requests"]
+    arrivals = np.cumsum(rng.exponential(1.0 / w["rate"], n_req))
+    reqs = []
+    for k in range(n_req):
+        j = int(rng.integers(0, len(scenes)))
+        S = float(sizes[j])
+        a, el = rng.uniform(0, 2 * np.pi), rng.uniform(0.35, 0.7)
+        eye = [S / 2 + 1.4 * S * np.cos(el) * np.cos(a), S / 2 + 1.4 * S * np.sin(el), S / 2 + 1.4 * S * np.cos(el) * np.sin(a)]
+        target = [S / 2 + rng.uniform(-0.1, 0.1) * S, S / 2, S / 2 + rng.uniform(-0.1, 0.1) * S]
+        wd, ht = RESOLUTIONS[int(rng.integers(0, len(RESOLUTIONS)))]
+        reqs.append((j, eye, target, 60.0, wd, ht))
+    total_rays = sum(r[4] * r[5] for r in reqs)
+    # pinned result buffers (status + albedo per ray), reused round-robin by later requests
+    ring = 48
+    maxn = max(r[4] * r[5] for r in reqs)
+    bufs = [{"status": torch.empty(maxn, dtype=torch.uint8).pin_memory().numpy(),
+             "albedo": torch.empty(maxn, dtype=torch.int32).pin_memory().numpy()} for _ in range(ring)]
+
+    def serve(srv, paced):
+        ids = [srv.add_scene(t) for t in scenes]
+        assert ids == list(range(len(scenes)))
+        # warm-up: every scene resident and the launch path exercised once
+        for j in range(len(scenes)):
+            srv.wait(srv.submit(j, [0.0, float(sizes[j]), 0.0], [sizes[j] / 2] * 3, 60.0, 64, 64,
+                                out={k: v[:4096] for k, v in bufs[0].items()}))
+        start = srv.now()
+        rids = []
+        for k, r in enumerate(reqs):
+            if paced:
+                delay = start + arrivals[k] - srv.now()
+                if delay > 0:
+                    time.sleep(delay)
+            out = {kk: v[:r[4] * r[5]] for kk, v in bufs[k % ring].items()}
+            rids.append(srv.submit(*r, out=out))
+        res = [srv.wait(i, 600.0) for i in rids]
+        lat = np.array([x["done_s"] - x["submit_s"] for x in res])
+        span = max(x["done_s"] for x in res) - min(x["submit_s"] for x in res)
+        st = srv.stats()
+        srv.close()
+        return {"value": round(total_rays / span / 1e6, 3), "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 2),
+                "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 2), "span_s": round(span, 3),
+                "launches": st["launches"], "uploads": st["uploads"], "evictions": st["evictions"],
+                "mean_batch": round(float(np.mean([x["batch_requests"] for x in res])), 2)}
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    budget = int(w["budget_gb"] * (1 << 30))
+    batched = serve(svo.Server(budget_bytes=budget, max_batch_requests=64, max_batch_rays=1 << 25, max_inflight=3),
+                    paced=True)
+    serial = serve(svo.Server(budget_bytes=budget, max_batch_requests=1, max_inflight=1), paced=True)
+    clk = clocks.stop()
+    print(json.dumps({
+        "metric": "Mrays/s", "value": batched["value"], "unit": "Mrays/s", "n_gpus": 1, "steps": n_req, "warmup": len(scenes),
+        "ms_per_step": round(batched["span_s"] / n_req * 1e3, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "served16", "scenes": len(scenes), "sizes": sizes, "requests": n_req,
+                   "arrival_rate_per_s": w["rate"], "rays": total_rays, "budget_gb": w["budget_gb"],
+                   "build_s": round(build_s, 1), "outputs": "status + albedo per ray, to pinned host memory",
+                   "served": batched, "serial_dispatch": serial,
+                   "p50_ms": batched["p50_ms"], "p99_ms": batched["p99_ms"]},
+        "roofline": None, "cpu_baseline": None,
+        "e2e": {"value": batched["value"], "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(total_rays * 5 / n_req)},
+        "gpu_launches": batched["launches"], "clocks": clk,
+    }))
+
+
 def run_reference(args, w):
     rank, _, world = dist_env()
     if rank != 0:
@@ -260,7 +542,16 @@ def main():
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
+        if "multi" in w or "served" in w:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the default single-scene workload"}))
+            return
         run_reference(args, w)
+        return
+    if "multi" in w:
+        run_multiscene(args, w)
+        return
+    if "served" in w:
+        run_served(args, w)
         return
 
     rank, local_rank, world = dist_env()

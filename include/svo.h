@@ -189,9 +189,58 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
 svo_status svo_cast_batched_noalloc(const svo_batch_item* items, uint32_t n_items, const svo_launch_config* cfg,
                                     void* stream);
 
+/* ---- serving: continuous batching of camera requests over resident scenes ---- */
+typedef struct svo_server svo_server;
+
+typedef struct {
+  uint64_t budget_bytes;        /* device memory for resident scene images; LRU scenes are evicted above it */
+  uint32_t max_batch_requests;  /* requests admitted into one launch (1..128) */
+  uint32_t max_batch_rays;      /* rays admitted into one launch (a single larger request still runs alone) */
+  uint32_t max_inflight;        /* launches in flight at once (1..4), each on its own stream */
+  svo_launch_config launch;     /* persistent-kernel launch configuration (0 = defaults) */
+} svo_server_config;
+
+/* A pinhole camera request: width*height rays generated on the device exactly as
+ * svo_gen_camera_rays generates them, cast against the scene, results copied to
+ * the caller's HOST buffers (any field may be NULL).  The buffers must stay valid
+ * until the request completes. */
+typedef struct {
+  uint32_t scene_id;
+  float eye[3], target[3], fov_deg;
+  uint32_t width, height;
+  svo_hits hits;
+} svo_request;
+
+typedef struct {
+  int32_t status;          /* SVO_OK, or the error that failed the request */
+  double submit_s, start_s, done_s; /* server clock: submitted, launched, results in host memory */
+  uint32_t batch_requests; /* requests that shared its launch */
+} svo_request_result;
+
+typedef struct {
+  uint64_t requests_done, rays_done, launches, uploads, evictions;
+  uint64_t resident_bytes;
+} svo_server_stats;
+
+/* Starts the server and its worker thread on the current device. */
+svo_status svo_server_create(const svo_server_config* cfg, svo_server** out);
+/* Stops the worker after the requests in flight complete and releases the server's device memory. */
+void svo_server_destroy(svo_server* server);
+/* Registers a scene (not owned; the caller keeps it alive and leaves it untouched while registered).
+ * The server uploads and evicts its device image under the budget. */
+svo_status svo_server_add_scene(svo_server* server, svo_scene* scene, uint32_t* scene_id);
+/* Queues a request; returns at once with its id. */
+svo_status svo_server_submit(svo_server* server, const svo_request* request, uint64_t* request_id);
+/* Waits up to timeout_s seconds for a request; SVO_ERR_BUSY on timeout. */
+svo_status svo_server_wait(svo_server* server, uint64_t request_id, double timeout_s, svo_request_result* out);
+svo_status svo_server_stats_get(svo_server* server, svo_server_stats* out);
+/* Seconds on the server clock (the clock of svo_request_result). */
+double svo_server_now(svo_server* server);
+
 /* ---- synthetic workloads (seeded, deterministic on x86_64 and aarch64) ---- */
 typedef struct {
-  uint32_t kind;      /* 0 heightfield+spheres, 1 terrain+caves, 2 sparse+uniform blocks, 3 noise+spheres */
+  uint32_t kind;      /* 0 heightfield+spheres, 1 terrain+caves, 2 sparse+uniform blocks, 3 noise+spheres,
+                         4 boxes of insert_at_lod cubes */
   uint32_t size, brick_dim;
   uint64_t seed;
   float occupancy;    /* target fraction for kinds 2 and 3 */

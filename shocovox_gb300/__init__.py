@@ -12,10 +12,11 @@ import ctypes
 
 import numpy as np
 
-from ._lib import (HIT_FIELDS, OP_DTYPE, Hits, LaunchConfig, Rays, SceneRecipe, check, lib)
+from ._lib import (HIT_FIELDS, OP_DTYPE, Hits, LaunchConfig, Rays, Request, RequestResult, SceneRecipe, ServerConfig,
+                   ServerStats, check, lib)
 
 __all__ = ["Octree", "OctreeError", "OP_DTYPE", "HIT_FIELDS", "gen_scene", "gen_camera_rays", "gen_sphere_rays",
-           "SceneRecipe", "LaunchConfig", "BatchWorkspace", "lib"]
+           "SceneRecipe", "LaunchConfig", "BatchWorkspace", "Server", "lib"]
 
 OK, INVALID_SIZE, INVALID_BRICK_DIM, INVALID_STRUCTURE, INVALID_POSITION = 0, 1, 2, 3, 4
 
@@ -191,6 +192,64 @@ class BatchWorkspace:
             arr[i].hits = Hits(**{k: _vp(hits.get(k, 0) or 0) for k in HIT_FIELDS})
         c = cfg if cfg is not None else LaunchConfig()
         check(lib().svo_cast_batched(self._h, arr, len(items), ctypes.byref(c), _vp(stream)))
+
+
+class Server:
+    """Continuous-batching request server over resident scenes (svo_server_*)."""
+
+    def __init__(self, budget_bytes=60 << 30, max_batch_requests=64, max_batch_rays=1 << 25, max_inflight=2,
+                 launch=None):
+        cfg = ServerConfig(budget_bytes, max_batch_requests, max_batch_rays, max_inflight,
+                           launch if launch is not None else LaunchConfig())
+        h = ctypes.c_void_p()
+        check(lib().svo_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self._scenes = []
+        self._keep = {}
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().svo_server_destroy(h)
+            self._h = None
+            self._keep.clear()
+
+    def __del__(self):
+        self.close()
+
+    def add_scene(self, scene):
+        sid = ctypes.c_uint32()
+        check(lib().svo_server_add_scene(self._h, scene.handle, ctypes.byref(sid)))
+        self._scenes.append(scene)  # keep it alive while registered
+        return sid.value
+
+    def submit(self, scene_id, eye, target, fov_deg, width, height, out):
+        """out: {field: host array of width*height}; the arrays must stay alive until wait()."""
+        r = Request(scene_id, (ctypes.c_float * 3)(*eye), (ctypes.c_float * 3)(*target), fov_deg, width, height,
+                    Hits(**{k: _vp(out[k].ctypes.data) if k in out else None for k in HIT_FIELDS}))
+        rid = ctypes.c_uint64()
+        check(lib().svo_server_submit(self._h, ctypes.byref(r), ctypes.byref(rid)))
+        self._keep[rid.value] = out
+        return rid.value
+
+    def wait(self, request_id, timeout_s=60.0):
+        res = RequestResult()
+        rc = lib().svo_server_wait(self._h, request_id, timeout_s, ctypes.byref(res))
+        if rc == 12:  # SVO_ERR_BUSY: still running
+            return None
+        self._keep.pop(request_id, None)
+        if rc != 0:
+            raise OctreeError(rc, lib().svo_last_error().decode())
+        return {"submit_s": res.submit_s, "start_s": res.start_s, "done_s": res.done_s,
+                "batch_requests": res.batch_requests}
+
+    def stats(self):
+        st = ServerStats()
+        check(lib().svo_server_stats_get(self._h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def now(self):
+        return lib().svo_server_now(self._h)
 
 
 def gen_scene(kind, size, brick_dim, seed, occupancy=0.1, spheres=0, octaves=2, base_freq=1.0 / 32,

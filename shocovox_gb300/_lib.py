@@ -50,6 +50,27 @@ class LaunchConfig(ctypes.Structure):
                 ("reserved", ctypes.c_uint32)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("budget_bytes", ctypes.c_uint64), ("max_batch_requests", ctypes.c_uint32),
+                ("max_batch_rays", ctypes.c_uint32), ("max_inflight", ctypes.c_uint32), ("launch", LaunchConfig)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("scene_id", ctypes.c_uint32), ("eye", ctypes.c_float * 3), ("target", ctypes.c_float * 3),
+                ("fov_deg", ctypes.c_float), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("hits", Hits)]
+
+
+class RequestResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("submit_s", ctypes.c_double), ("start_s", ctypes.c_double),
+                ("done_s", ctypes.c_double), ("batch_requests", ctypes.c_uint32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_uint64) for k in ("requests_done", "rays_done", "launches", "uploads", "evictions",
+                                                "resident_bytes")]
+
+
 class BatchItem(ctypes.Structure):
     _fields_ = [("scene", ctypes.c_void_p), ("rays", Rays), ("n", ctypes.c_uint64), ("hits", Hits)]
 
@@ -82,6 +103,13 @@ SIGNATURES = {
     "svo_batch_workspace_destroy": (None, [_VP]),
     "svo_cast_batched": (_I32, [_VP, _P(BatchItem), _U32, _P(LaunchConfig), _VP]),
     "svo_cast_batched_noalloc": (_I32, [_P(BatchItem), _U32, _P(LaunchConfig), _VP]),
+    "svo_server_create": (_I32, [_P(ServerConfig), _P(_VP)]),
+    "svo_server_destroy": (None, [_VP]),
+    "svo_server_add_scene": (_I32, [_VP, _VP, _P(_U32)]),
+    "svo_server_submit": (_I32, [_VP, _P(Request), _P(_U64)]),
+    "svo_server_wait": (_I32, [_VP, _U64, ctypes.c_double, _P(RequestResult)]),
+    "svo_server_stats_get": (_I32, [_VP, _P(ServerStats)]),
+    "svo_server_now": (ctypes.c_double, [_VP]),
     "svo_gen_scene": (_I32, [_P(SceneRecipe), _VP, _U64, _P(_U64)]),
     "svo_gen_camera_rays": (_I32, [_P(_F), _P(_F), _F, _U32, _U32, _VP, _VP, _VP, _VP, _VP, _VP]),
     "svo_gen_sphere_rays": (_I32, [_P(_F), _F, _U64, _U64, _VP, _VP, _VP, _VP, _VP, _VP]),

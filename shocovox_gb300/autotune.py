@@ -1,0 +1,63 @@
+"""Autotuner of the persistent batched cast (svo_cast_batched).
+
+Sweeps threads per block, rays per warp grab and persistent CTAs per SM on the
+caller's own batch, keeps the fastest, and caches the choice per (GPU name,
+workload signature) in a JSON file next to the built library, so later runs
+skip the sweep.
+"""
+import json
+import os
+import time
+
+from . import _lib
+
+CACHE = os.path.join(os.path.dirname(_lib.lib_path()), "autotune_cache.json")
+BLOCKS = (64, 128, 256)
+CHUNKS = (32, 64, 128)
+PER_SM = (0,)  # 0 = as many as occupancy allows
+
+
+def _load():
+    try:
+        with open(CACHE) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(cache):
+    os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+    tmp = CACHE + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(cache, f, indent=1, sort_keys=True)
+    os.replace(tmp, CACHE)
+
+
+def signature(items):
+    """Workload class: item count and total rays (log2-bucketed), octree sizes and brick dims present."""
+    total = sum(n for _, _, n, _ in items)
+    sizes = sorted({s.size for s, _, _, _ in items})
+    dims = sorted({s.brick_dim for s, _, _, _ in items})
+    return "items%d_rays2^%d_sizes%s_dims%s" % (len(items), max(total, 1).bit_length(), sizes, dims)
+
+
+def tune(ws, items, gpu_name, time_fn, use_cache=True):
+    """Returns (LaunchConfig, table).  time_fn(cfg) -> milliseconds of one batched cast."""
+    key = "%s|%s" % (gpu_name, signature(items))
+    cache = _load() if use_cache else {}
+    if key in cache:
+        b, c, p = cache[key]["config"]
+        return _lib.LaunchConfig(b, c, p, 0), {"cached": True, **cache[key]}
+    table = {}
+    for b in BLOCKS:
+        for c in CHUNKS:
+            for p in PER_SM:
+                cfg = _lib.LaunchConfig(b, c, p, 0)
+                table["%dx%dx%d" % (b, c, p)] = time_fn(cfg)
+    best = min(table, key=table.get)
+    b, c, p = (int(v) for v in best.split("x"))
+    entry = {"config": [b, c, p], "ms": table[best], "sweep_ms": table, "when": time.strftime("%Y-%m-%dT%H:%M:%S")}
+    if use_cache:
+        cache[key] = entry
+        _store(cache)
+    return _lib.LaunchConfig(b, c, p, 0), {"cached": False, **entry}

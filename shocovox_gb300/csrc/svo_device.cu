@@ -36,6 +36,20 @@ __global__ void __launch_bounds__(128, 7) cast_kernel(SceneView s, RaysView rays
 int g_cast_mode = 0;
 
 // ------------------------------------------------------------------ device image
+uint64_t device_image_bytes(const svo_scene* sc) {
+  const DeviceImage& d = sc->dev;
+  if (!d.valid) return 0;
+  const uint64_t len = sc->tree.arena.len(), W = len >= 32 ? len / 32 : 1;
+  return d.node_cap * sizeof(DevNode) + d.brick_cap * (len + W) * 4 + (d.color_cap + d.data_cap) * 4;
+}
+uint64_t device_image_bytes_estimate(const svo_scene* sc) {
+  const HostOctree& t = sc->tree;
+  const uint64_t nn = t.nodes(), nb = std::max<uint64_t>(1, t.arena.slots());
+  const uint64_t nc = std::max<uint64_t>(1, t.colors.size()), nd = std::max<uint64_t>(1, t.datas.size());
+  const uint64_t len = t.arena.len(), W = len >= 32 ? len / 32 : 1;
+  return (nn + nn / 4 + 64) * sizeof(DevNode) + (nb + nb / 4 + 16) * (len + W) * 4 + (nc + nc / 4 + 64 + nd + nd / 4 + 64) * 4;
+}
+
 SceneView scene_view(const svo_scene* sc) {
   const DeviceImage& d = sc->dev;
   SceneView v;

@@ -68,6 +68,15 @@ struct svo_scene {
 };
 
 namespace svo {
+struct CameraFrame {
+  float fwd[3], right[3];
+  float tan_half, aspect;
+};
+void camera_frame(const float eye[3], const float target[3], float fov_deg, uint32_t width, uint32_t height,
+                  CameraFrame* out);
+// device image size in bytes: as allocated (uploaded scene) or as a full upload would allocate
+uint64_t device_image_bytes(const svo_scene* s);
+uint64_t device_image_bytes_estimate(const svo_scene* s);
 void set_error(const std::string& msg);
 svo_status fail(svo_status code, const std::string& msg);
 SceneView scene_view(const svo_scene* s);

@@ -301,7 +301,60 @@ void gen_sparse_blocks(const svo_scene_recipe& r, OpSink& sink) {
       }
 }
 
+// kind 4: axis-aligned boxes on a 2*brick_dim cell grid, each filled with insert_at_lod cubes of one
+// cell, until the target occupancy; every 20th box gets a noise-carved detail cell of single voxels
+// on top (mixed bricks).  Builds large sparse scenes with few operations.
+void gen_boxes(const svo_scene_recipe& r, OpSink& sink) {
+  const uint32_t S = r.size, cell = 2 * r.brick_dim, n = S / cell;
+  Pcg32 g(r.seed);
+  const uint32_t seed = (uint32_t)(r.seed * 3266489917ull);
+  const double target = (double)S * S * S * r.occupancy;
+  double placed = 0;
+  uint32_t box = 0;
+  while (placed < target && n >= 2) {
+    const uint32_t span = std::max(2u, n / 14);  // box sides of 1..span cells (1..9 at 2048^3, brick 8)
+    const uint32_t w = std::min(n, 1u + g.range(0, span)), h = std::min(n, 1u + g.range(0, span)),
+                   d = std::min(n, 1u + g.range(0, span));
+    const uint32_t x0 = g.range(0, n - w + 1), y0 = g.range(0, n - h + 1), z0 = g.range(0, n - d + 1);
+    const uint32_t color = q565(g), user = 1u + g.range(0, 255);
+    for (uint32_t x = x0; x < x0 + w; ++x)
+      for (uint32_t y = y0; y < y0 + h; ++y)
+        for (uint32_t z = z0; z < z0 + d; ++z) sink.add(SVO_OP_INSERT_AT_LOD, x * cell, y * cell, z * cell, cell, color, user);
+    placed += (double)w * h * d * cell * cell * cell;
+    if (box % 20 == 0 && y0 + h < n) {
+      const uint32_t cx = x0 * cell, cy = (y0 + h) * cell, cz = z0 * cell;
+      for (uint32_t x = 0; x < cell; ++x)
+        for (uint32_t y = 0; y < cell; ++y)
+          for (uint32_t z = 0; z < cell; ++z)
+            if (value_noise3((float)(cx + x) * 0.3f, (float)(cy + y) * 0.3f, (float)(cz + z) * 0.3f, seed) > 0.6f)
+              sink.add(SVO_OP_INSERT, cx + x, cy + y, cz + z, 1, color, user + 1);
+    }
+    ++box;
+  }
+}
+
 }  // namespace
+
+// Pinhole frame shared by the host and device ray generators: forward and right
+// axes (V3c::normalized, V3c::cross order of operations), tan(fov / 2) from the
+// fixed double-precision sin/cos above, and the aspect ratio.
+void camera_frame(const float eye[3], const float target[3], float fov_deg, uint32_t width, uint32_t height,
+                  CameraFrame* out) {
+  const V3 e{eye[0], eye[1], eye[2]};
+  const V3 fwd = normalized(sub(V3{target[0], target[1], target[2]}, e));
+  const V3 up{0.0f, 1.0f, 0.0f};  // examples/cpu_render.rs:83-86
+  const V3 right = normalized(cross(up, fwd));
+  double s, c;
+  det_sincos((double)fov_deg * kPi / 360.0, &s, &c);
+  out->fwd[0] = fwd.x;
+  out->fwd[1] = fwd.y;
+  out->fwd[2] = fwd.z;
+  out->right[0] = right.x;
+  out->right[1] = right.y;
+  out->right[2] = right.z;
+  out->tan_half = (float)(s / c);
+  out->aspect = (float)width / (float)height;
+}
 }  // namespace svo
 
 using namespace svo;
@@ -314,6 +367,8 @@ svo_status svo_gen_scene(const svo_scene_recipe* r, svo_op* ops, uint64_t max_op
   OpSink sink(ops, max_ops);
   if (r->kind == 2)
     gen_sparse_blocks(*r, sink);
+  else if (r->kind == 4)
+    gen_boxes(*r, sink);
   else
     gen_dense(*r, sink);
   *n_ops = sink.count();
@@ -324,23 +379,19 @@ svo_status svo_gen_camera_rays(const float eye[3], const float target[3], float 
                                uint32_t height, float* ox, float* oy, float* oz, float* dx, float* dy, float* dz) {
   if (!eye || !target || !ox || !oy || !oz || !dx || !dy || !dz || !width || !height)
     return fail(SVO_ERR_ARGUMENT, "svo_gen_camera_rays: bad argument");
-  const V3 e{eye[0], eye[1], eye[2]};
-  const V3 fwd = normalized(sub(V3{target[0], target[1], target[2]}, e));
+  CameraFrame f;
+  camera_frame(eye, target, fov_deg, width, height, &f);
+  const V3 fwd{f.fwd[0], f.fwd[1], f.fwd[2]}, right{f.right[0], f.right[1], f.right[2]};
   const V3 up{0.0f, 1.0f, 0.0f};  // examples/cpu_render.rs:83-86
-  const V3 right = normalized(cross(up, fwd));
-  double s, c;
-  det_sincos((double)fov_deg * kPi / 360.0, &s, &c);
-  const float th = (float)(s / c);
-  const float aspect = (float)width / (float)height;
   for (uint32_t py = 0; py < height; ++py)
     for (uint32_t px = 0; px < width; ++px) {
-      const float u = (2.0f * ((float)px + 0.5f) / (float)width - 1.0f) * th * aspect;
-      const float v = (1.0f - 2.0f * ((float)py + 0.5f) / (float)height) * th;
+      const float u = (2.0f * ((float)px + 0.5f) / (float)width - 1.0f) * f.tan_half * f.aspect;
+      const float v = (1.0f - 2.0f * ((float)py + 0.5f) / (float)height) * f.tan_half;
       const V3 d = normalized(add(add(fwd, mul(right, u)), mul(up, v)));
       const size_t i = (size_t)py * width + px;
-      ox[i] = e.x;
-      oy[i] = e.y;
-      oz[i] = e.z;
+      ox[i] = eye[0];
+      oy[i] = eye[1];
+      oz[i] = eye[2];
       dx[i] = d.x;
       dy[i] = d.y;
       dz[i] = d.z;

@@ -1,0 +1,112 @@
+"""The serving loop: results equal single casts alone and in a mix; budget eviction; timeouts and bad ids."""
+import numpy as np
+import pytest
+
+import shocovox_gb300 as svo
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("status", "entry_kind", "node_key", "voxel_index", "albedo", "user", "px", "py", "pz", "nx", "ny", "nz")
+
+
+def scenes():
+    out = []
+    for j, (kind, size, dim) in enumerate([(0, 64, 4), (3, 128, 8), (1, 64, 2)]):
+        ops = svo.gen_scene(kind, size, dim, seed=500 + j, occupancy=0.1, spheres=3, octaves=2, base_freq=1.0 / 16,
+                            height_lo=2.0, height_hi=size * 0.35)
+        t = svo.Octree(size, dim)
+        t.apply_ops(ops)
+        out.append(t)
+    return out
+
+
+def requests(sc, rng, n):
+    reqs = []
+    for i in range(n):
+        j = int(rng.integers(0, len(sc)))
+        S = float(sc[j].size)
+        a = rng.uniform(0, 2 * np.pi)
+        eye = [S / 2 + 1.5 * S * np.cos(a), 1.1 * S, S / 2 + 1.5 * S * np.sin(a)]
+        w, h = [(32, 24), (64, 48), (160, 120), (7, 5)][i % 4]
+        reqs.append((j, eye, [S / 2, S / 3, S / 2], 60.0, w, h))
+    return reqs
+
+
+def out_arrays(w, h):
+    return {k: np.zeros(w * h, dtype=svo.HIT_FIELDS[k]) for k in FIELDS}
+
+
+def expected(sc, req):
+    j, eye, target, fov, w, h = req
+    o, d = svo.gen_camera_rays(eye, target, fov, w, h)
+    sc[j].upload()
+    return sc[j].cast_host(o, d, fields=FIELDS)
+
+
+def same(a, b):
+    for k in FIELDS:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_server_results_are_the_same_alone_and_in_the_mix():
+    sc = scenes()
+    reqs = requests(sc, np.random.default_rng(1), 24)
+    ref = [expected(sc, r) for r in reqs]
+    srv = svo.Server(budget_bytes=1 << 34, max_batch_requests=8, max_inflight=2)
+    ids = [srv.add_scene(t) for t in sc]
+    assert ids == [0, 1, 2]
+    # alone: one request in the server at a time
+    for r, e in zip(reqs, ref):
+        out = out_arrays(r[4], r[5])
+        res = srv.wait(srv.submit(*r, out=out))
+        assert res["batch_requests"] == 1
+        same(out, e)
+    # in the mix: all submitted at once, batched and overlapped by the server
+    outs = [out_arrays(r[4], r[5]) for r in reqs]
+    rids = [srv.submit(*r, out=o) for r, o in zip(reqs, outs)]
+    results = [srv.wait(i) for i in rids]
+    assert max(x["batch_requests"] for x in results) > 1
+    for o, e in zip(outs, ref):
+        same(o, e)
+    st = srv.stats()
+    assert st["requests_done"] == 48 and st["launches"] < 48
+    srv.close()
+
+
+def test_server_evicts_under_a_small_budget_and_stays_correct():
+    sc = scenes()
+    for t in sc:
+        t.release_device()
+    reqs = requests(sc, np.random.default_rng(2), 12)
+    ref = [expected(sc, r) for r in reqs]
+    for t in sc:
+        t.release_device()
+    srv = svo.Server(budget_bytes=1, max_batch_requests=1, max_inflight=1)
+    for t in sc:
+        srv.add_scene(t)
+    outs = [out_arrays(r[4], r[5]) for r in reqs]
+    rids = [srv.submit(*r, out=o) for r, o in zip(reqs, outs)]
+    for i in rids:
+        srv.wait(i)
+    for o, e in zip(outs, ref):
+        same(o, e)
+    st = srv.stats()
+    assert st["evictions"] > 0 and st["uploads"] > len(sc)
+    srv.close()
+
+
+def test_server_rejects_unknown_scene_and_reports_timeouts():
+    sc = scenes()[:1]
+    srv = svo.Server(max_inflight=1)
+    srv.add_scene(sc[0])
+    with pytest.raises(RuntimeError):
+        srv.submit(5, [0, 0, 0], [1, 1, 1], 60.0, 4, 4, out={})
+    big = out_arrays(1920, 1080)
+    rid = srv.submit(0, [200.0, 90.0, 200.0], [32.0, 20.0, 32.0], 60.0, 1920, 1080, out=big)
+    res = srv.wait(rid, timeout_s=0.0)  # a deadline that has already passed: not ready yet (or just done)
+    if res is None:
+        res = srv.wait(rid, timeout_s=60.0)
+    assert res["done_s"] >= res["start_s"] >= res["submit_s"]
+    with pytest.raises(RuntimeError):
+        srv.wait(rid)  # a request is waited for once
+    srv.close()
