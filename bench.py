@@ -328,13 +328,14 @@ def run_multiscene(args, w):
     clk = clocks.stop()
 
     # algorithmic bytes of the batch, from the instrumented batched cast
-    cnt = [{k: torch.zeros(n, dtype=torch.int32, device=dev) for k in ("status", "node_visits", "child_reads",
-                                                                        "voxel_reads")} for (_, _, n, _, _) in items]
+    cnt = [dict(status=torch.zeros(n, dtype=torch.uint8, device=dev),
+                **{k: torch.zeros(n, dtype=torch.int32, device=dev) for k in ("node_visits", "child_reads", "voxel_reads")})
+           for (_, _, n, _, _) in items]
     citems = [(t, rp, n, {k: v.data_ptr() for k, v in c.items()}) for (t, rp, n, _, _), c in zip(items, cnt)]
     ws.cast(citems, cfg, s)
     torch.cuda.synchronize()
     sums = {k: sum(int(c[k].to(torch.int64).sum()) for c in cnt) for k in ("node_visits", "child_reads", "voxel_reads")}
-    hits = sum(int(((c["status"] & 0xFF) == 1).sum()) for c in cnt)
+    hits = sum(int((c["status"] == 1).sum()) for c in cnt)
     alg = 12 * sums["node_visits"] + 4 * sums["child_reads"] + 4 * sums["voxel_reads"] + 8 * hits
 
     # end to end: host rays in, one batched launch, host hits out (pinned buffers, copies in the timed region)
