@@ -415,7 +415,7 @@ def run_served(args, w):
     import shocovox_gb300 as svo
     torch.cuda.set_device(0)
     rng = np.random.default_rng(w["seed"])
-    sizes = [int(rng.choice([256, 512, 1024, 2048])) for _ in range(w["served"])]
+    sizes = [int(v) for v in rng.permutation(np.repeat([256, 512, 1024, 2048], w["served"] // 4))]
     t0 = time.perf_counter()
     scenes = []
     for i, S in enumerate(sizes):

@@ -86,10 +86,12 @@ __device__ __forceinline__ float offz(uint32_t o) { return (float)((o >> 1) & 1u
 struct Bounds {
   float x, y, z, s, inv;
 };
-// Cube::child_bounds_for (src/spatial/mod.rs:32-39)
+// Cube::child_bounds_for (src/spatial/mod.rs:32-39).  offset * half is half or +0 (offsets are 0 or 1)
+// and minima are >= 0, so selecting the addend gives the reference's sums bit for bit.
 __device__ __forceinline__ Bounds child_bounds(const Bounds& b, uint32_t o) {
   const float h = b.s * 0.5f;
-  return Bounds{b.x + offx(o) * h, b.y + offy(o) * h, b.z + offz(o) * h, h, b.inv * 2.0f};
+  return Bounds{b.x + ((o & 1u) ? h : 0.0f), b.y + ((o & 4u) ? h : 0.0f), b.z + ((o & 2u) ? h : 0.0f), h,
+                b.inv * 2.0f};
 }
 
 struct RayState {
