@@ -568,9 +568,11 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
           }
         }
       }
-      const float rx = (r.px - cb.x) * 4.0f * cb.inv;
-      const float ry = (r.py - cb.y) * 4.0f * cb.inv;
-      const float rz = (r.pz - cb.z) * 4.0f * cb.inv;
+      // (x * 4) / size == x * (4 / size): both only rescale x by powers of two
+      const float q4 = cb.inv * 4.0f;
+      const float rx = (r.px - cb.x) * q4;
+      const float ry = (r.py - cb.y) * q4;
+      const float rz = (r.pz - cb.z) * q4;
       uint32_t flat = min(__float2uint_rz(rx), 3u) + 4u * min(__float2uint_rz(ry), 3u) +
                       16u * min(__float2uint_rz(rz), 3u);
       if (backtrack || target == kOob || occ == 0 || (occ & rtn[flat * 8u]) == 0) {
@@ -613,7 +615,7 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
         float bx = rclamp(rx, kTol, 4.0f - kTol);
         float by = rclamp(ry, kTol, 4.0f - kTol);
         float bz = rclamp(rz, kTol, 4.0f - kTol);
-        const float dbx = g4x * cb.inv, dby = g4y * cb.inv, dbz = g4z * cb.inv;
+        const float dbx = (g4x > 0.0f) ? q4 : -q4, dby = (g4y > 0.0f) ? q4 : -q4, dbz = (g4z > 0.0f) ? q4 : -q4;
         for (;;) {
           if (++work > kWorkCap) {
             h.status = 2;
