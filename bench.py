@@ -200,7 +200,7 @@ def batched_variants(svo, torch, scene, rp, hp, n, stream, args):
         return e0.elapsed_time(e1) / reps
 
     sweep = []
-    for block in (64, 128, 256):
+    for block in (64, 96, 128):
         for chunk in (32, 64, 256):
             cfg = svo.LaunchConfig(block, chunk, 0, 0)
             sweep.append(((block, chunk), timed(cfg, 2)))
@@ -312,7 +312,7 @@ def run_multiscene(args, w):
     same = all(torch.equal(a[k], b[k]) for a, b in zip(ref_out, outs) for k in OUT_FIELDS)
     # one persistent launch captured in a CUDA graph (workspace already sized, blocks per SM fixed)
     if cfg.blocks_per_sm == 0:
-        per_sm = {64: 16, 128: 7, 256: 3}.get(cfg.block, 2)
+        per_sm = {64: 14, 96: 9, 128: 7}.get(cfg.block, 2)
         gcfg = svo.LaunchConfig(cfg.block, cfg.rays_per_chunk, per_sm, 0)
     else:
         gcfg = cfg

@@ -160,7 +160,7 @@ typedef struct {
 } svo_batch_item;
 
 typedef struct {
-  uint32_t block;          /* threads per block (multiple of 32, <= 1024); 0 = default 128 */
+  uint32_t block;          /* threads per block (multiple of 32, <= 128); 0 = default 128 */
   uint32_t rays_per_chunk; /* rays a warp claims per work-queue grab; 0 = default 64 */
   uint32_t blocks_per_sm;  /* persistent CTAs per SM; 0 = default from occupancy */
   uint32_t reserved;

@@ -12,7 +12,7 @@ import time
 from . import _lib
 
 CACHE = os.path.join(os.path.dirname(_lib.lib_path()), "autotune_cache.json")
-BLOCKS = (64, 128, 256)
+BLOCKS = (64, 96, 128)
 CHUNKS = (32, 64, 128)
 PER_SM = (0,)  # 0 = as many as occupancy allows
 

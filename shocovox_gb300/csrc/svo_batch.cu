@@ -31,9 +31,14 @@ struct BatchItemDev {
 
 constexpr uint32_t kMaxSharedItems = 1024;  // prefix sums staged in shared memory
 
+// At most kBatchMaxBlock threads per block with 6 resident blocks per SM (80 registers, a few
+// spilled bytes); the launch configuration is checked against the block limit.
+constexpr uint32_t kBatchMaxBlock = 128;
+
 template <bool kCount>
-__global__ void batched_kernel(const BatchItemDev* __restrict__ items, uint32_t n_items, uint64_t total,
-                               unsigned long long* __restrict__ counter, uint32_t chunk) {
+__global__ void __launch_bounds__(kBatchMaxBlock, 6)
+    batched_kernel(const BatchItemDev* __restrict__ items, uint32_t n_items, uint64_t total,
+                   unsigned long long* __restrict__ counter, uint32_t chunk) {
   __shared__ uint64_t s_begin[kMaxSharedItems];
   __shared__ SharedLuts L;
   const uint32_t staged = n_items < kMaxSharedItems ? n_items : kMaxSharedItems;
@@ -187,7 +192,8 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
   if (total == 0) return SVO_OK;
   const uint32_t block = (cfg && cfg->block) ? cfg->block : 128;
   const uint32_t chunk = (cfg && cfg->rays_per_chunk) ? cfg->rays_per_chunk : 64;
-  if (block % 32 != 0 || block > 1024 || chunk == 0) return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: bad launch config");
+  if (block % 32 != 0 || block > kBatchMaxBlock || chunk == 0)
+    return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: block must be a multiple of 32 and at most 128");
   int per_sm = (cfg && cfg->blocks_per_sm) ? (int)cfg->blocks_per_sm : 0;
   if (per_sm == 0) {
     if (count)
@@ -290,8 +296,8 @@ svo_status svo_cast_batched_noalloc(const svo_batch_item* items, uint32_t n_item
   if (total == 0) return SVO_OK;
   const uint32_t block = (cfg && cfg->block) ? cfg->block : 128;
   const uint32_t chunk = (cfg && cfg->rays_per_chunk) ? cfg->rays_per_chunk : 64;
-  if (block % 32 != 0 || block > 1024 || chunk == 0)
-    return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: bad launch config");
+  if (block % 32 != 0 || block > kBatchMaxBlock || chunk == 0)
+    return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: block must be a multiple of 32 and at most 128");
   int per_sm = (cfg && cfg->blocks_per_sm) ? (int)cfg->blocks_per_sm : 0;
   if (per_sm == 0) {
     if (count)

@@ -259,7 +259,7 @@ def test_batched_multi_scene_matches_single_scene_casts(oracle_mod):
         scenes.append(p)
         keep.append((cols, out))
     ws = svo.BatchWorkspace()
-    for cfg in (svo.LaunchConfig(0, 0, 0, 0), svo.LaunchConfig(256, 32, 1, 0), svo.LaunchConfig(64, 512, 2, 0)):
+    for cfg in (svo.LaunchConfig(0, 0, 0, 0), svo.LaunchConfig(128, 32, 1, 0), svo.LaunchConfig(64, 512, 2, 0)):
         for _, out in keep:
             for v in out.values():
                 v.zero_()
