@@ -43,6 +43,7 @@ WORKLOADS = {
 }
 RESOLUTIONS = [(320, 240), (640, 480), (1280, 720), (1920, 1080), (3840, 2160)]
 OUT_FIELDS = ("status", "entry_kind", "albedo", "user", "px", "py", "pz", "nx", "ny", "nz")
+COUNTERS = ("node_visits", "child_reads", "voxel_reads", "run_visits")
 OUT_BYTES = {"status": 1, "entry_kind": 1, "albedo": 4, "user": 4, "px": 4, "py": 4, "pz": 4, "nx": 4, "ny": 4,
              "nz": 4}
 
@@ -145,6 +146,13 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def alg_bytes_of(performed_visits, child_reads, voxel_reads, hits):
+    """Algorithmic bytes of a cast: 12 B (occupancy bits + node kind) per node visit the cast performs,
+    4 B per child key read, 4 B per voxel tested, 8 B (albedo + user) per hit.  Restart visits that the
+    cast counts in closed form read nothing and are left out (performed = node_visits - run_visits)."""
+    return 12 * performed_visits + 4 * child_reads + 4 * voxel_reads + 8 * hits
 
 
 def dist_env():
@@ -263,19 +271,27 @@ def run_multiscene(args, w):
     stream = torch.cuda.current_stream(dev)
     s = stream.cuda_stream
     tmap = {np.uint8: torch.uint8, np.uint32: torch.int32, np.float32: torch.float32}
-    scenes, items, host_rays, outs = [], [], [], []
-    for sp, (t, _) in zip(specs, built):
+    # one batch: every ray column and hit field is one buffer over all scenes, each scene a slice
+    ray_keys = ("ox", "oy", "oz", "dx", "dy", "dz")
+    host_rays = [multiscene_rays(svo, sp) for sp in specs]
+    counts = [len(o) for o, _ in host_rays]
+    begins = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    total = int(begins[-1])
+    all_o = np.concatenate([o for o, _ in host_rays])
+    all_d = np.concatenate([d for _, d in host_rays])
+    host_cols = [np.ascontiguousarray(all_o[:, i]) for i in range(3)] + [np.ascontiguousarray(all_d[:, i]) for i in range(3)]
+    dev_cols = {k: torch.from_numpy(c).to(dev) for k, c in zip(ray_keys, host_cols)}
+    dev_out = {k: torch.empty(total, dtype=tmap[svo.HIT_FIELDS[k]], device=dev) for k in OUT_FIELDS}
+    scenes, items, outs = [], [], []
+    for i, (t, _) in enumerate(built):
         t.upload(s)
-        o, d = multiscene_rays(svo, sp)
-        cols = [np.ascontiguousarray(o[:, i]) for i in range(3)] + [np.ascontiguousarray(d[:, i]) for i in range(3)]
-        rays = {k: torch.from_numpy(c).to(dev) for k, c in zip(("ox", "oy", "oz", "dx", "dy", "dz"), cols)}
-        out = {k: torch.empty(len(o), dtype=tmap[svo.HIT_FIELDS[k]], device=dev) for k in OUT_FIELDS}
+        a, b = int(begins[i]), int(begins[i + 1])
+        rays = {k: v[a:b] for k, v in dev_cols.items()}
+        out = {k: v[a:b] for k, v in dev_out.items()}
         scenes.append(t)
-        host_rays.append((o, d, cols))
         outs.append(out)
-        items.append((t, {k: v.data_ptr() for k, v in rays.items()}, len(o),
+        items.append((t, {k: v.data_ptr() for k, v in rays.items()}, b - a,
                       {k: v.data_ptr() for k, v in out.items()}, rays))
-    total = sum(it[2] for it in items)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     def timed(fn, reps):
@@ -312,7 +328,7 @@ def run_multiscene(args, w):
     same = all(torch.equal(a[k], b[k]) for a, b in zip(ref_out, outs) for k in OUT_FIELDS)
     # one persistent launch captured in a CUDA graph (workspace already sized, blocks per SM fixed)
     if cfg.blocks_per_sm == 0:
-        per_sm = {64: 14, 96: 9, 128: 7}.get(cfg.block, 2)
+        per_sm = {64: 12, 96: 8, 128: 6}.get(cfg.block, 2)  # resident blocks at 80 registers per thread
         gcfg = svo.LaunchConfig(cfg.block, cfg.rays_per_chunk, per_sm, 0)
     else:
         gcfg = cfg
@@ -329,28 +345,26 @@ def run_multiscene(args, w):
 
     # algorithmic bytes of the batch, from the instrumented batched cast
     cnt = [dict(status=torch.zeros(n, dtype=torch.uint8, device=dev),
-                **{k: torch.zeros(n, dtype=torch.int32, device=dev) for k in ("node_visits", "child_reads", "voxel_reads")})
+                **{k: torch.zeros(n, dtype=torch.int32, device=dev) for k in COUNTERS})
            for (_, _, n, _, _) in items]
     citems = [(t, rp, n, {k: v.data_ptr() for k, v in c.items()}) for (t, rp, n, _, _), c in zip(items, cnt)]
     ws.cast(citems, cfg, s)
     torch.cuda.synchronize()
-    sums = {k: sum(int(c[k].to(torch.int64).sum()) for c in cnt) for k in ("node_visits", "child_reads", "voxel_reads")}
+    sums = {k: sum(int(c[k].to(torch.int64).sum()) for c in cnt) for k in COUNTERS}
     hits = sum(int((c["status"] == 1).sum()) for c in cnt)
-    alg = 12 * sums["node_visits"] + 4 * sums["child_reads"] + 4 * sums["voxel_reads"] + 8 * hits
+    alg = alg_bytes_of(sums["node_visits"] - sums["run_visits"], sums["child_reads"], sums["voxel_reads"], hits)
 
-    # end to end: host rays in, one batched launch, host hits out (pinned buffers, copies in the timed region)
-    pin_in = [[torch.from_numpy(c).pin_memory() for c in cols] for (_, _, cols) in host_rays]
-    pin_out = [{k: torch.empty(len(o), dtype=tmap[svo.HIT_FIELDS[k]]).pin_memory() for k in OUT_FIELDS}
-               for (o, _, _) in host_rays]
+    # end to end: host rays in, one batched launch, host hits out (pinned buffers, copies in the timed region;
+    # one copy per ray column and per hit field of the whole batch)
+    pin_in = {k: torch.from_numpy(c).pin_memory() for k, c in zip(ray_keys, host_cols)}
+    pin_out = {k: torch.empty(total, dtype=tmap[svo.HIT_FIELDS[k]]).pin_memory() for k in OUT_FIELDS}
 
     def e2e():
-        for (_, _, _, _, rays), pins in zip(items, pin_in):
-            for k, p in zip(("ox", "oy", "oz", "dx", "dy", "dz"), pins):
-                rays[k].copy_(p, non_blocking=True)
+        for k in ray_keys:
+            dev_cols[k].copy_(pin_in[k], non_blocking=True)
         ws.cast(bitems, cfg, s)
-        for out, po in zip(outs, pin_out):
-            for k in OUT_FIELDS:
-                po[k].copy_(out[k], non_blocking=True)
+        for k in OUT_FIELDS:
+            pin_out[k].copy_(dev_out[k], non_blocking=True)
 
     e2e()
     torch.cuda.synchronize()
@@ -373,7 +387,7 @@ def run_multiscene(args, w):
                                 spheres=sp["spheres"], octaves=sp["octaves"], base_freq=sp["base_freq"])
             ot = oracle.Tree(sp["size"], sp["brick_dim"])
             ot.apply_ops(ops)
-            o, d, _ = host_rays[i]
+            o, d = host_rays[i]
             step = max(1, len(o) // 20000)
             tt = time.perf_counter()
             ot.cast(o[::step], d[::step], threads=threads)
@@ -594,13 +608,13 @@ def main():
     torch.cuda.synchronize()
 
     # algorithmic bytes of one launch from the instrumented cast (counters equal the oracle's, see tests)
-    cnt = {k: torch.empty(n, dtype=torch.int32, device=dev) for k in ("node_visits", "child_reads", "voxel_reads")}
+    cnt = {k: torch.empty(n, dtype=torch.int32, device=dev) for k in COUNTERS}
     st = torch.empty(n, dtype=torch.uint8, device=dev)
     scene.cast(rp, dict(status=st.data_ptr(), **{k: v.data_ptr() for k, v in cnt.items()}), n, s)
     torch.cuda.synchronize()
-    visits, creads, vreads = (int(cnt[k].to(torch.int64).sum()) for k in ("node_visits", "child_reads", "voxel_reads"))
+    visits, creads, vreads, runs = (int(cnt[k].to(torch.int64).sum()) for k in COUNTERS)
     hits = int((st == 1).sum())
-    alg_bytes = 12 * visits + 4 * creads + 4 * vreads + 8 * hits
+    alg_bytes = alg_bytes_of(visits - runs, creads, vreads, hits)
     del cnt
 
     if pg:
@@ -667,7 +681,7 @@ def main():
             "config": {"workload": args.workload, "octree": "%d^3" % w["size"], "brick_dim": w["brick_dim"],
                        "rays_per_step": n, "hit_rate": round(hits / n, 4), "nodes": st["nodes"],
                        "per_ray": {"node_visits": round(visits / n, 2), "child_reads": round(creads / n, 2),
-                                   "voxel_reads": round(vreads / n, 2)},
+                                   "voxel_reads": round(vreads / n, 2), "restart_run_visits": round(runs / n, 2)},
                        "parted_bricks": st["parted_bricks"], "voxels_inserted": int(len(ops)),
                        "l2": "inputs larger than L2 (rays %.0f MB + hits %.0f MB per step); the %.0f MB scene image "
                              "stays resident" % (n * 24 / 1e6, n * sum(OUT_BYTES.values()) / 1e6,

@@ -92,6 +92,8 @@ typedef struct {
   uint32_t* node_visits; /* optional instrumentation counters */
   uint32_t* child_reads;
   uint32_t* voxel_reads;
+  uint32_t* run_visits;  /* of node_visits, the restart visits that the cast counted without performing them one
+                            by one (runs of restarts whose root test fails; no counterpart in the reference) */
 } svo_hits;
 
 typedef struct {

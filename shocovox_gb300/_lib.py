@@ -21,6 +21,7 @@ HIT_FIELDS = {
     "voxel_index": np.uint32, "pix": np.uint32, "albedo": np.uint32, "user": np.uint32,
     "px": np.float32, "py": np.float32, "pz": np.float32, "nx": np.float32, "ny": np.float32,
     "nz": np.float32, "node_visits": np.uint32, "child_reads": np.uint32, "voxel_reads": np.uint32,
+    "run_visits": np.uint32,
 }
 
 

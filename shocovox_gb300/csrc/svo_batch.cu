@@ -72,36 +72,11 @@ __global__ void __launch_bounds__(kBatchMaxBlock, 6)
       cast_one<kCount>(it.scene, L, __ldg(r.ox + i), __ldg(r.oy + i), __ldg(r.oz + i), __ldg(r.dx + i),
                        __ldg(r.dy + i), __ldg(r.dz + i), h);
       write_hit(it.scene, it.hits, i, h);
-      if (kCount) {
-        if (it.hits.visits) it.hits.visits[i] = h.visits;
-        if (it.hits.creads) it.hits.creads[i] = h.creads;
-        if (it.hits.vreads) it.hits.vreads[i] = h.vreads;
-      }
+      if (kCount) write_counters(it.hits, i, h);
     }
   }
 }
 
-HitsView hits_view_of(const svo_hits& h) {
-  HitsView v;
-  v.status = h.status;
-  v.octant = h.brick_octant;
-  v.kind = h.entry_kind;
-  v.node = h.node_key;
-  v.voxel = h.voxel_index;
-  v.pix = h.pix;
-  v.albedo = h.albedo;
-  v.user = h.user;
-  v.px = h.px;
-  v.py = h.py;
-  v.pz = h.pz;
-  v.nx = h.nx;
-  v.ny = h.ny;
-  v.nz = h.nz;
-  v.visits = h.node_visits;
-  v.creads = h.child_reads;
-  v.vreads = h.voxel_reads;
-  return v;
-}
 
 }  // namespace svo
 
@@ -187,7 +162,7 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
     d.begin = total;
     d.n = it.n;
     total += it.n;
-    count |= it.hits.node_visits || it.hits.child_reads || it.hits.voxel_reads;
+    count |= counts_requested(it.hits);
   }
   if (total == 0) return SVO_OK;
   const uint32_t block = (cfg && cfg->block) ? cfg->block : 128;
@@ -291,7 +266,7 @@ svo_status svo_cast_batched_noalloc(const svo_batch_item* items, uint32_t n_item
     d.begin = total;
     d.n = it.n;
     total += it.n;
-    count |= it.hits.node_visits || it.hits.child_reads || it.hits.voxel_reads;
+    count |= counts_requested(it.hits);
   }
   if (total == 0) return SVO_OK;
   const uint32_t block = (cfg && cfg->block) ? cfg->block : 128;

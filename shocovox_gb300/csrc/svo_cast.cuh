@@ -14,6 +14,7 @@
 #include <string>
 
 #include "svo_internal.h"
+#include "svo_restart.h"
 
 namespace svo {
 
@@ -44,7 +45,7 @@ __device__ __forceinline__ int isignum(int v) { return (v > 0) - (v < 0); }
 // ------------------------------------------------------------------ look-up tables as arithmetic
 // RAY_TO_NODE_OCCUPANCY_BITMASK_LUT[pos][dir] (src/spatial/lut.rs:33-84, 255-896): the 4x4x4 box
 // between cell pos = x + 4y + 16z and the far corner in direction octant dir.
-__device__ __forceinline__ uint64_t ray_to_node_mask(uint32_t pos, uint32_t dir) {
+__host__ __device__ constexpr uint64_t ray_to_node_mask(uint32_t pos, uint32_t dir) {
   const uint32_t x = pos & 3u, y = (pos >> 2) & 3u, z = (pos >> 4) & 3u;
   const uint32_t xm = (dir & 1u) ? ((0xFu << x) & 0xFu) : (0xFu >> (3u - x));
   const uint32_t ym = (dir & 4u) ? ((0xFu << y) & 0xFu) : (0xFu >> (3u - y));
@@ -57,7 +58,7 @@ __device__ __forceinline__ uint64_t ray_to_node_mask(uint32_t pos, uint32_t dir)
   return X & Y & Z;
 }
 // BITMAP_MASK_FOR_OCTANT_LUT (lut.rs:199-208): the 2x2x2 block of octant o
-__device__ __forceinline__ uint64_t octant_mask(uint32_t o) {
+__host__ __device__ constexpr uint64_t octant_mask(uint32_t o) {
   const uint64_t X = (uint64_t)(3u << (2u * (o & 1u))) * 0x1111111111111111ull;
   const uint64_t Y = (uint64_t)(0xFFu << (8u * ((o >> 2) & 1u))) * 0x0001000100010001ull;
   const uint64_t Z = 0xFFFFFFFFull << (32u * ((o >> 1) & 1u));
@@ -147,7 +148,7 @@ __device__ __forceinline__ void impact_normal(const Bounds& c, float px, float p
 struct HitRecord {
   uint32_t status, octant, node, voxel, pix;
   float px, py, pz, nx, ny, nz;
-  uint32_t visits, creads, vreads;
+  uint32_t visits, creads, vreads, runs;  // counters, kept only by the instrumented cast
 };
 
 enum : uint32_t { kKindNothing = 0, kKindInternal = 1, kKindLeaf = 2, kKindUniform = 3 };
@@ -220,13 +221,23 @@ __device__ __forceinline__ bool bitmap_index(float bx, float by, float bz, uint3
 
 // RAY_TO_NODE_OCCUPANCY_BITMASK_LUT and BITMAP_MASK_FOR_OCTANT_LUT staged in
 // shared memory by each block (computed with the arithmetic above).
-struct SharedLuts {
+struct alignas(16) SharedLuts {
   uint64_t ray_to_node[512];  // [pos * 8 + dir]
   uint64_t octant[8];
 };
+// The tables, evaluated at compile time into each module's global memory; a block copies them
+// into shared memory with 16-byte loads (two per thread at 128 threads).
+constexpr SharedLuts make_luts() {
+  SharedLuts t{};
+  for (uint32_t i = 0; i < 512; ++i) t.ray_to_node[i] = ray_to_node_mask(i >> 3, i & 7u);
+  for (uint32_t o = 0; o < 8; ++o) t.octant[o] = octant_mask(o);
+  return t;
+}
+static __device__ const SharedLuts kLuts = make_luts();
 __device__ __forceinline__ void fill_shared_luts(SharedLuts& L) {
-  for (uint32_t i = threadIdx.x; i < 512; i += blockDim.x) L.ray_to_node[i] = ray_to_node_mask(i >> 3, i & 7u);
-  if (threadIdx.x < 8) L.octant[threadIdx.x] = octant_mask(threadIdx.x);
+  const uint4* src = reinterpret_cast<const uint4*>(&kLuts);
+  uint4* dst = reinterpret_cast<uint4*>(&L);
+  for (uint32_t i = threadIdx.x; i < sizeof(SharedLuts) / 16; i += blockDim.x) dst[i] = __ldg(src + i);
 }
 
 // Octree::get_by_ray (raytracing_on_cpu.rs:316-565, MIP maps disabled)
@@ -239,7 +250,7 @@ __device__ void cast_ray(const SceneView& s, const SharedLuts& L, float ox, floa
   h.voxel = 0xFFFFFFFFu;
   h.pix = 0;
   h.px = h.py = h.pz = h.nx = h.ny = h.nz = 0.0f;
-  if (kCount) h.visits = h.creads = h.vreads = 0;
+  if (kCount) h.visits = h.creads = h.vreads = h.runs = 0;
 
   RayState r;
   r.dx = dx;
@@ -393,6 +404,22 @@ __device__ void cast_ray(const SceneView& s, const SharedLuts& L, float ox, floa
   }
 }
 
+// restart_cells_run out of line: it runs a few times per ray at most, and inlined it would add to
+// the register allocation of the whole traversal loop.
+struct RestartRun {
+  float x, y, z;
+  uint32_t k;
+};
+static __device__ __noinline__ RestartRun restart_run(float x, float y, float z, float cx, float cy, float cz, uint32_t flat,
+                                                      float w, uint32_t n_max) {
+  RestartRun o;
+  o.k = restart_cells_run(x, y, z, cx, cy, cz, flat, w, n_max);
+  o.x = x;
+  o.y = y;
+  o.z = z;
+  return o;
+}
+
 // ---------------------------------------------------------------------------
 // Fast form of the same cast for directions without NaN (signum is +-1 on every
 // axis).  It performs the reference's operations on every value it keeps; only
@@ -501,7 +528,7 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
   h.voxel = 0xFFFFFFFFu;
   h.pix = 0;
   h.px = h.py = h.pz = h.nx = h.ny = h.nz = 0.0f;
-  if (kCount) h.visits = h.creads = h.vreads = 0;
+  if (kCount) h.visits = h.creads = h.vreads = h.runs = 0;
 
   FastRay r;
   r.dx = dx;
@@ -642,9 +669,43 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
         }
       }
     }
-    r.px = r.px + dx * 0.1f;
-    r.py = r.py + dy * 0.1f;
-    r.pz = r.pz + dz * 0.1f;
+    const float c01x = dx * 0.1f, c01y = dy * 0.1f, c01z = dz * 0.1f;  // the same product on every restart
+    r.px = r.px + c01x;
+    r.py = r.py + c01y;
+    r.pz = r.pz + c01z;
+    // Restarts whose root visit fails its occupancy test (an Internal or empty root, whose visit
+    // neither probes nor pushes) repeat visit, POP and nudge until the point changes root bitmap
+    // cell; each such run is taken in closed form, counting its visits.
+    const uint4 root = __ldg(reinterpret_cast<const uint4*>(s.nodes));
+    const uint64_t occ_root = ((uint64_t)root.y << 32) | root.x;
+    const bool root_runs = (root.z & 3u) == kKindInternal || (root.z & 3u) == kKindNothing;
+    const float q4r = s.inv_size * 4.0f;
+    while (root_runs && r.px < S && r.py < S && r.pz < S && r.px > 0.0f && r.py > 0.0f && r.pz > 0.0f) {
+      const float rx = (r.px - 0.0f) * q4r, ry = (r.py - 0.0f) * q4r, rz = (r.pz - 0.0f) * q4r;
+      const uint32_t flat = min(__float2uint_rz(rx), 3u) + 4u * min(__float2uint_rz(ry), 3u) +
+                            16u * min(__float2uint_rz(rz), 3u);
+      if (occ_root != 0 && (occ_root & rtn[flat * 8u]) != 0) break;
+      if (++work > kWorkCap) {
+        h.status = 2;
+        return;
+      }
+      if (kCount) h.visits++;
+      // the visits before the next cell change fail alike; the cap holds if they fit in it
+      const RestartRun run = restart_run(r.px, r.py, r.pz, c01x, c01y, c01z, flat, S * 0.25f, kWorkCap - work + 2u);
+      const uint32_t k = run.k;
+      r.px = run.x;
+      r.py = run.y;
+      r.pz = run.z;
+      if (k == kRunNever) {
+        h.status = 2;
+        return;
+      }
+      work += k - 1u;
+      if (kCount) {
+        h.visits += k - 1u;
+        h.runs += k - 1u;
+      }
+    }
     target = (r.px < S && r.py < S && r.pz < S && r.px > 0.0f && r.py > 0.0f && r.pz > 0.0f)
                  ? hash_region(r.px, r.py, r.pz, S * 0.5f)
                  : kOob;
@@ -673,8 +734,31 @@ struct HitsView {
   uint8_t *status, *octant, *kind;
   uint32_t *node, *voxel, *pix, *albedo, *user;
   float *px, *py, *pz, *nx, *ny, *nz;
-  uint32_t *visits, *creads, *vreads;
+  uint32_t *visits, *creads, *vreads, *runs;
 };
+
+__host__ __device__ inline HitsView hits_view_of(const svo_hits& h) {
+  HitsView v;
+  v.status = h.status;
+  v.octant = h.brick_octant;
+  v.kind = h.entry_kind;
+  v.node = h.node_key;
+  v.voxel = h.voxel_index;
+  v.pix = h.pix;
+  v.albedo = h.albedo;
+  v.user = h.user;
+  v.px = h.px;
+  v.py = h.py;
+  v.pz = h.pz;
+  v.nx = h.nx;
+  v.ny = h.ny;
+  v.nz = h.nz;
+  v.visits = h.node_visits;
+  v.creads = h.child_reads;
+  v.vreads = h.voxel_reads;
+  v.runs = h.run_visits;
+  return v;
+}
 
 __device__ __forceinline__ void write_hit(const SceneView& s, const HitsView& o, uint64_t i, HitRecord& h) {
   uint32_t kind = 0, albedo = 0, user = 0;
@@ -703,7 +787,7 @@ __device__ __forceinline__ void write_hit(const SceneView& s, const HitsView& o,
     h.px = h.py = h.pz = h.nx = h.ny = h.nz = 0.0f;
     kind = albedo = user = 0;
   }
-  if (h.status >= 2) h.visits = h.creads = h.vreads = 0;  // no defined counts past a cap or panic
+  if (h.status >= 2) h.visits = h.creads = h.vreads = h.runs = 0;  // no defined counts past a cap or panic
   if (o.status) o.status[i] = (uint8_t)h.status;
   if (o.octant) o.octant[i] = (uint8_t)h.octant;
   if (o.kind) o.kind[i] = (uint8_t)kind;
@@ -718,6 +802,13 @@ __device__ __forceinline__ void write_hit(const SceneView& s, const HitsView& o,
   if (o.nx) o.nx[i] = h.nx;
   if (o.ny) o.ny[i] = h.ny;
   if (o.nz) o.nz[i] = h.nz;
+}
+
+__device__ __forceinline__ void write_counters(const HitsView& o, uint64_t i, const HitRecord& h) {
+  if (o.visits) o.visits[i] = h.visits;
+  if (o.creads) o.creads[i] = h.creads;
+  if (o.vreads) o.vreads[i] = h.vreads;
+  if (o.runs) o.runs[i] = h.runs;
 }
 
 

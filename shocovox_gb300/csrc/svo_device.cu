@@ -26,11 +26,7 @@ __global__ void __launch_bounds__(128, 7) cast_kernel(SceneView s, RaysView rays
   cast_one<kCount>(s, L, __ldg(rays.ox + i), __ldg(rays.oy + i), __ldg(rays.oz + i), __ldg(rays.dx + i),
                    __ldg(rays.dy + i), __ldg(rays.dz + i), h);
   write_hit(s, out, i, h);
-  if (kCount) {
-    if (out.visits) out.visits[i] = h.visits;
-    if (out.creads) out.creads[i] = h.creads;
-    if (out.vreads) out.vreads[i] = h.vreads;
-  }
+  if (kCount) write_counters(out, i, h);
 }
 
 int g_cast_mode = 0;
@@ -234,34 +230,13 @@ svo_status incremental_sync(svo_scene* sc, cudaStream_t st) {
   return SVO_OK;
 }
 
-HitsView hits_view(const svo_hits* h) {
-  HitsView v;
-  v.status = h->status;
-  v.octant = h->brick_octant;
-  v.kind = h->entry_kind;
-  v.node = h->node_key;
-  v.voxel = h->voxel_index;
-  v.pix = h->pix;
-  v.albedo = h->albedo;
-  v.user = h->user;
-  v.px = h->px;
-  v.py = h->py;
-  v.pz = h->pz;
-  v.nx = h->nx;
-  v.ny = h->ny;
-  v.nz = h->nz;
-  v.visits = h->node_visits;
-  v.creads = h->child_reads;
-  v.vreads = h->voxel_reads;
-  return v;
-}
 
 svo_status launch_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_hits* hits, cudaStream_t st) {
   if (n == 0) return SVO_OK;
   const SceneView v = scene_view(sc);
   RaysView rv{rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz};
-  const HitsView hv = hits_view(hits);
-  const bool count = hits->node_visits || hits->child_reads || hits->voxel_reads;
+  const HitsView hv = hits_view_of(*hits);
+  const bool count = counts_requested(*hits);
   const unsigned block = 128;
   const uint64_t grid = (n + block - 1) / block;
   if (grid > 0x7FFFFFFFull) return fail(SVO_ERR_ARGUMENT, "svo_cast: too many rays for one launch");
@@ -278,7 +253,6 @@ svo_status launch_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const sv
 // device->host copy overlap chunk i's kernel (with pinned host memory; with
 // pageable memory the copies still run, only without overlap).
 constexpr int kPipeStreams = 3;
-constexpr size_t kFieldBytes[17] = {1, 1, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4};
 
 struct HostPipeline {
   cudaStream_t st[kPipeStreams] = {};
@@ -308,8 +282,8 @@ svo_status cast_host_pipelined(svo_scene* sc, const svo_rays* rays, uint64_t n, 
   DeviceImage& d = sc->dev;
   void* const* host_fields = reinterpret_cast<void* const*>(hits);
   size_t per_ray = 24;
-  for (int f = 0; f < 17; ++f)
-    if (host_fields[f]) per_ray += kFieldBytes[f];
+  for (int f = 0; f < kHitFields; ++f)
+    if (host_fields[f]) per_ray += kHitFieldBytes[f];
   const uint64_t chunk = std::min<uint64_t>(n, std::max<uint64_t>(262144, ((n / 6 + 255) / 256) * 256));
   const size_t need = (size_t)chunk * per_ray + 32 * 256;
   HostPipeline* p = static_cast<HostPipeline*>(d.ws);
@@ -353,18 +327,18 @@ svo_status cast_host_pipelined(svo_scene* sc, const svo_rays* rays, uint64_t n, 
     svo_hits dh;
     std::memset(&dh, 0, sizeof(dh));
     void** dev_fields = reinterpret_cast<void**>(&dh);
-    for (int f = 0; f < 17; ++f)
+    for (int f = 0; f < kHitFields; ++f)
       if (host_fields[f]) {
         dev_fields[f] = base + o;
-        o += ((kFieldBytes[f] * chunk + 255) / 256) * 256;
+        o += ((kHitFieldBytes[f] * chunk + 255) / 256) * 256;
       }
     svo_rays drays{dr[0], dr[1], dr[2], dr[3], dr[4], dr[5]};
     svo_status rc = launch_cast(sc, &drays, m, &dh, st);
     if (rc != SVO_OK) return rc;
-    for (int f = 0; f < 17; ++f)
+    for (int f = 0; f < kHitFields; ++f)
       if (host_fields[f])
-        SVO_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(host_fields[f]) + off * kFieldBytes[f], dev_fields[f],
-                                     kFieldBytes[f] * m, cudaMemcpyDeviceToHost, st));
+        SVO_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(host_fields[f]) + off * kHitFieldBytes[f], dev_fields[f],
+                                     kHitFieldBytes[f] * m, cudaMemcpyDeviceToHost, st));
   }
   for (int i = 0; i < kPipeStreams; ++i) {
     SVO_CUDA_TRY(cudaEventRecord(p->done[i], p->st[i]));
@@ -377,10 +351,14 @@ svo_status cast_host_pipelined(svo_scene* sc, const svo_rays* rays, uint64_t n, 
 }  // namespace
 
 // ------------------------------------------------------------------ LUT self-test kernel
+// Reports the tables exactly as a cast block holds them in shared memory.
 __global__ void lut_kernel(uint64_t* rtn, uint32_t* step, uint64_t* mask) {
+  __shared__ SharedLuts L;
+  fill_shared_luts(L);
+  __syncthreads();
   const uint32_t t = threadIdx.x;
-  if (t < 512) rtn[t] = ray_to_node_mask(t >> 3, t & 7u);
-  if (t < 8) mask[t] = octant_mask(t);
+  if (t < 512) rtn[t] = L.ray_to_node[t];
+  if (t < 8) mask[t] = L.octant[t];
   if (t < 27) {  // OCTANT_STEP_RESULT_LUT[x][y][z] packs 8 octants x 4 bits
     const int x = (int)(t / 9) - 1, y = (int)((t / 3) % 3) - 1, z = (int)(t % 3) - 1;
     uint32_t packed = 0;

@@ -24,6 +24,14 @@ static_assert(sizeof(DevNode) == 64, "DevNode must be 64 bytes");
 
 constexpr uint32_t kInvalidChild = 0xFFFFFFFFu;
 
+// svo_hits is an array of kHitFields pointers; bytes per ray of each field, in declaration order.
+constexpr int kHitFields = 18;
+constexpr size_t kHitFieldBytes[kHitFields] = {1, 1, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4};
+static_assert(sizeof(svo_hits) == kHitFields * sizeof(void*), "svo_hits must hold only the field pointers");
+inline bool counts_requested(const svo_hits& h) {
+  return h.node_visits || h.child_reads || h.voxel_reads || h.run_visits;
+}
+
 // Everything a cast kernel needs to read one scene (all device pointers).
 struct SceneView {
   const DevNode* nodes;

@@ -39,7 +39,6 @@ namespace {
     }                                                                                             \
   } while (0)
 
-constexpr size_t kFieldBytes[17] = {1, 1, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4};
 
 struct CamParams {
   float ex, ey, ez;
@@ -170,8 +169,8 @@ svo_status launch(svo_server* sv, LaunchSlot& ls, size_t n_scenes, LaunchCounts&
     total += q->n;
     need += ((q->n * 24 + 255) / 256) * 256 + 6 * 256;
     void* const* hf = reinterpret_cast<void* const*>(&q->r.hits);
-    for (int f = 0; f < 17; ++f)
-      if (hf[f]) need += ((kFieldBytes[f] * q->n + 255) / 256) * 256;
+    for (int f = 0; f < kHitFields; ++f)
+      if (hf[f]) need += ((kHitFieldBytes[f] * q->n + 255) / 256) * 256;
   }
   if (need > ls.bytes) {
     SRV_CUDA(cudaStreamSynchronize(ls.st));
@@ -206,10 +205,10 @@ svo_status launch(svo_server* sv, LaunchSlot& ls, size_t n_scenes, LaunchCounts&
     it.n = q->n;
     void* const* hf = reinterpret_cast<void* const*>(&q->r.hits);
     void** df = reinterpret_cast<void**>(&it.hits);
-    for (int fi = 0; fi < 17; ++fi)
+    for (int fi = 0; fi < kHitFields; ++fi)
       if (hf[fi]) {
         df[fi] = ls.buf + o;
-        o += ((kFieldBytes[fi] * q->n + 255) / 256) * 256;
+        o += ((kHitFieldBytes[fi] * q->n + 255) / 256) * 256;
       }
   }
   rc = svo_cast_batched(ls.ws, items.data(), (uint32_t)items.size(), &sv->cfg.launch, ls.st);
@@ -218,8 +217,8 @@ svo_status launch(svo_server* sv, LaunchSlot& ls, size_t n_scenes, LaunchCounts&
     Request* q = ls.reqs[i];
     void* const* hf = reinterpret_cast<void* const*>(&q->r.hits);
     void** df = reinterpret_cast<void**>(&items[i].hits);
-    for (int f = 0; f < 17; ++f)
-      if (hf[f]) SRV_CUDA(cudaMemcpyAsync(hf[f], df[f], kFieldBytes[f] * q->n, cudaMemcpyDeviceToHost, ls.st));
+    for (int f = 0; f < kHitFields; ++f)
+      if (hf[f]) SRV_CUDA(cudaMemcpyAsync(hf[f], df[f], kHitFieldBytes[f] * q->n, cudaMemcpyDeviceToHost, ls.st));
   }
   SRV_CUDA(cudaEventRecord(ls.done, ls.st));
   cnt.launches++;
