@@ -40,6 +40,10 @@ WORKLOADS = {
                            rays=("sphere", 1 << 22)),
     "multiscene64": dict(multi=64, seed=0x5EED0004),
     "served16": dict(served=16, seed=0x5EED0005, rate=2000.0, requests=600, budget_gb=60.0),
+    # the terrain512 scene seen through examples/cpu_render.rs's viewport: fused ray generation + cast + shading
+    "viewport512": dict(viewport=4, kind=1, size=512, brick_dim=8, seed=0x5EED0002, spheres=0, octaves=3,
+                        base_freq=1.0 / 128, height_lo=0.02 * S_TERRAIN, height_hi=0.33 * S_TERRAIN,
+                        cave_threshold=0.55, width=1920, height=1080),
 }
 RESOLUTIONS = [(320, 240), (640, 480), (1280, 720), (1920, 1080), (3840, 2160)]
 OUT_FIELDS = ("status", "entry_kind", "albedo", "user", "px", "py", "pz", "nx", "ny", "nz")
@@ -464,15 +468,18 @@ def run_served(args, w):
             srv.wait(srv.submit(j, [0.0, float(sizes[j]), 0.0], [sizes[j] / 2] * 3, 60.0, 64, 64,
                                 out={k: v[:4096] for k, v in bufs[0].items()}))
         start = srv.now()
-        rids = []
+        rids, res = [], [None] * len(reqs)
         for k, r in enumerate(reqs):
+            if k >= ring:  # the result buffers of request k - ring are reused: it must be done
+                res[k - ring] = srv.wait(rids[k - ring], 600.0)
             if paced:
                 delay = start + arrivals[k] - srv.now()
                 if delay > 0:
                     time.sleep(delay)
             out = {kk: v[:r[4] * r[5]] for kk, v in bufs[k % ring].items()}
             rids.append(srv.submit(*r, out=out))
-        res = [srv.wait(i, 600.0) for i in rids]
+        for k in range(max(0, len(reqs) - ring), len(reqs)):
+            res[k] = srv.wait(rids[k], 600.0)
         lat = np.array([x["done_s"] - x["submit_s"] for x in res])
         span = max(x["done_s"] for x in res) - min(x["submit_s"] for x in res)
         st = srv.stats()
@@ -488,6 +495,10 @@ def run_served(args, w):
     batched = serve(svo.Server(budget_bytes=budget, max_batch_requests=64, max_batch_rays=1 << 25, max_inflight=3),
                     paced=True)
     serial = serve(svo.Server(budget_bytes=budget, max_batch_requests=1, max_inflight=1), paced=True)
+    # capacity: the same requests submitted as fast as result buffers free up (48 in flight)
+    batched_cap = serve(svo.Server(budget_bytes=budget, max_batch_requests=64, max_batch_rays=1 << 25,
+                                   max_inflight=3), paced=False)
+    serial_cap = serve(svo.Server(budget_bytes=budget, max_batch_requests=1, max_inflight=1), paced=False)
     clk = clocks.stop()
     print(json.dumps({
         "metric": "Mrays/s", "value": batched["value"], "unit": "Mrays/s", "n_gpus": 1, "steps": n_req, "warmup": len(scenes),
@@ -497,11 +508,148 @@ def run_served(args, w):
                    "arrival_rate_per_s": w["rate"], "rays": total_rays, "budget_gb": w["budget_gb"],
                    "build_s": round(build_s, 1), "outputs": "status + albedo per ray, to pinned host memory",
                    "served": batched, "serial_dispatch": serial,
+                   "capacity": {"note": "all requests queued, 48 outstanding", "served": batched_cap,
+                                "serial_dispatch": serial_cap},
                    "p50_ms": batched["p50_ms"], "p99_ms": batched["p99_ms"]},
         "roofline": None, "cpu_baseline": None,
         "e2e": {"value": batched["value"], "unit": "Mrays/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": int(total_rays * 5 / n_req)},
         "gpu_launches": batched["launches"], "clocks": clk,
+    }))
+
+
+def viewport_rays(vp, W, H):
+    """The rays of svo_render_viewport's pixels in image order (row 0 = top), formed on the host with
+    examples/cpu_render.rs's f32 operations (the device forms the same bits)."""
+    F = np.float32
+
+    def norm(v):
+        n = np.sqrt((v[..., 0] * v[..., 0] + v[..., 1] * v[..., 1]) + v[..., 2] * v[..., 2])
+        return v / n[..., None]
+    o, d, up = (np.array(list(getattr(vp, k)), F) for k in ("origin", "direction", "up"))
+    right = norm(np.array([up[1] * d[2] - up[2] * d[1], up[2] * d[0] - up[0] * d[2], up[0] * d[1] - up[1] * d[0]], F))
+    pw, ph = F(vp.width) / F(W), F(vp.height) / F(H)
+    bl = ((o + d * F(vp.fov)) - up * (F(vp.height) / F(2))) - right * (F(vp.width) / F(2))
+    x = np.arange(W, dtype=F)[None, :, None]
+    y = np.arange(H, dtype=F)[:, None, None]
+    dirs = norm(((bl + (right * x) * pw) + (up * y) * ph) - o)[::-1].reshape(-1, 3)
+    return np.ascontiguousarray(np.broadcast_to(o, dirs.shape)), np.ascontiguousarray(dirs)
+
+
+def run_viewport(args, w):
+    """Fused render (svo_render_viewport) of 4 orbit viewports vs the plain cast of the same rays."""
+    import torch
+    import shocovox_gb300 as svo
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    t0 = time.perf_counter()
+    ops = scene_ops(svo, w)
+    scene = svo.Octree(w["size"], w["brick_dim"])
+    scene.apply_ops(ops)
+    build_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream(dev)
+    s = stream.cuda_stream
+    scene.upload(s)
+    S, W, H = float(w["size"]), w["width"], w["height"]
+    rng = np.random.default_rng(w["seed"])
+    vps = []
+    for _ in range(w["viewport"]):
+        v = svo.orbit_viewport(rng.uniform(0, 2 * np.pi), 1.1 * S)
+        o = np.array(list(v.origin), np.float32) + np.float32(S / 2)
+        d = np.array([S / 2, 0.2 * S, S / 2], np.float32) - o
+        d = d / np.sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2], dtype=np.float32)
+        vps.append(svo.viewport(o, d, fov=2.0))
+    n = W * H * len(vps)
+    img = torch.empty((len(vps), H, W, 4), dtype=torch.uint8, device=dev)
+    bad = torch.zeros(1, dtype=torch.int64, device=dev)
+    pin = torch.empty((len(vps), H, W, 4), dtype=torch.uint8).pin_memory()
+
+    def render():
+        for k, vp in enumerate(vps):
+            scene.render_viewport(vp, W, H, img[k].data_ptr(), bad.data_ptr(), s)
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(0)
+    clocks.start()
+    for _ in range(args.warmup):
+        render()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        render()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    # end to end: the frames land in pinned host memory every step
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        render()
+        pin.copy_(img, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t1) / args.steps
+    clk = clocks.stop()
+
+    # the same rays through the plain cast (rays resident in HBM), and the algorithmic bytes
+    host = [viewport_rays(vp, W, H) for vp in vps]
+    o_all = np.concatenate([h[0] for h in host])
+    d_all = np.concatenate([h[1] for h in host])
+    cols = [np.ascontiguousarray(o_all[:, i]) for i in range(3)] + [np.ascontiguousarray(d_all[:, i]) for i in range(3)]
+    rays = {k: torch.from_numpy(c).to(dev) for k, c in zip(("ox", "oy", "oz", "dx", "dy", "dz"), cols)}
+    rp = {k: v.data_ptr() for k, v in rays.items()}
+    tmap = {np.uint8: torch.uint8, np.uint32: torch.int32, np.float32: torch.float32}
+    outs = {k: torch.empty(n, dtype=tmap[svo.HIT_FIELDS[k]], device=dev) for k in ("status", "albedo", "nx", "ny", "nz")}
+    hp = {k: v.data_ptr() for k, v in outs.items()}
+    for _ in range(args.warmup):
+        scene.cast(rp, hp, n, s)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        scene.cast(rp, hp, n, s)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    cast_ms = e0.elapsed_time(e1) / args.steps
+    cnt = {k: torch.empty(n, dtype=torch.int32, device=dev) for k in COUNTERS}
+    st = torch.empty(n, dtype=torch.uint8, device=dev)
+    scene.cast(rp, dict(status=st.data_ptr(), **{k: v.data_ptr() for k, v in cnt.items()}), n, s)
+    torch.cuda.synchronize()
+    visits, creads, vreads, runs = (int(cnt[k].to(torch.int64).sum()) for k in COUNTERS)
+    hits = int((st == 1).sum())
+    # a fused pixel reads the scene like its cast and writes 4 bytes instead of 24 B in + hit fields out
+    alg = alg_bytes_of(visits - runs, creads, vreads, hits) + 4 * n
+    del cnt, rays, outs
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle
+        ot = oracle.Tree(w["size"], w["brick_dim"])
+        ot.apply_ops(ops)
+        threads = os.cpu_count() or 1
+        rate, m, stride, dt = cpu_cast_rate(ot, o_all, d_all, args.cpu_seconds, threads)
+        cpu = {"value": round(rate / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": "every %dth pixel ray of the 4 frames (%d rays, %.1fs on %d threads), cast only" % (
+                   stride, m, dt, threads)}
+    peak, peak_src = measured_peak()
+    achieved = alg / (ms / 1e3) / 1e9
+    print(json.dumps({
+        "metric": "Mrays/s", "value": round(n / (ms / 1e3) / 1e6, 3), "unit": "Mrays/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "viewport512", "octree": "%d^3" % w["size"], "brick_dim": w["brick_dim"],
+                   "frames_per_step": len(vps), "resolution": [W, H], "rays_per_step": n, "hit_rate": round(hits / n, 4),
+                   "per_ray": {"node_visits": round(visits / n, 2), "child_reads": round(creads / n, 2),
+                               "voxel_reads": round(vreads / n, 2), "restart_run_visits": round(runs / n, 2)},
+                   "build_s": round(build_s, 1), "unshaded_pixels": int(bad.item()),
+                   "l2": "frames %.0f MB per step (larger than L2); the scene image stays resident" % (n * 4 / 1e6),
+                   "cast_of_same_rays": {"value": round(n / (cast_ms / 1e3) / 1e6, 3), "ms_per_step": round(cast_ms, 4),
+                                         "note": "svo_cast, rays resident in HBM, status+albedo+normal out"}},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_src,
+                     "alg_bytes_per_launch": alg // len(vps), "alg_bytes_per_ray": round(alg / n, 2)},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(n / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": n * 4},
+        "gpu_launches": args.steps * len(vps), "clocks": clk,
     }))
 
 
@@ -557,7 +705,7 @@ def main():
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
-        if "multi" in w or "served" in w:
+        if "multi" in w or "served" in w or "viewport" in w:
             print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the default single-scene workload"}))
             return
         run_reference(args, w)
@@ -567,6 +715,9 @@ def main():
         return
     if "served" in w:
         run_served(args, w)
+        return
+    if "viewport" in w:
+        run_viewport(args, w)
         return
 
     rank, local_rank, world = dist_env()

@@ -146,12 +146,41 @@ svo_status svo_scene_sync(svo_scene* scene, void* stream);
 svo_status svo_scene_release_device(svo_scene* scene);
 
 /* ---- the hot path: Octree::get_by_ray (src/raytracing/raytracing_on_cpu.rs:316-565) ---- */
-/* n rays in device memory -> per-ray hits in device memory.  Allocates nothing. */
+/* n rays in device memory -> per-ray hits in device memory.  Allocates nothing.
+ * Batches of 32768 rays and more run as a work queue: warps claim 32 rays at a time from a
+ * counter that the scene keeps per stream (up to 64 streams; casts on further streams, and on
+ * cudaStreamPerThread, use one thread per ray).  Casts of one scene on different streams may
+ * overlap.  A CUDA graph that captured a cast reuses the counter of the stream it was captured
+ * on: do not run it concurrently with casts on that stream. */
 svo_status svo_cast(svo_scene* scene, const svo_rays* rays, uint64_t n, const svo_hits* hits, void* stream);
 /* Same cast with host (ideally pinned) ray and hit buffers: host->device copy,
  * cast, device->host copy, stream synchronised before return.  Uses a
  * per-scene device workspace that grows on demand. */
 svo_status svo_cast_host(svo_scene* scene, const svo_rays* rays, uint64_t n, const svo_hits* hits, void* stream);
+
+/* ---- fused viewport render: examples/cpu_render.rs:77-138 on the device ---- */
+/* The example's frame: a viewport of width x height world units at distance fov in front of
+ * origin along direction (unit length, as the example makes it), right = normalize(up x
+ * direction); pixel (x, y) casts from origin towards bottom_left + right * x * (width / W) +
+ * up * y * (height / H), bottom_left = origin + direction * fov - up * height / 2 -
+ * right * width / 2.  A hit is shaded 1 - (normal . light / 2 + 0.5) times its albedo's r, g,
+ * b (cast to u8), alpha 255; a miss gets background.  The example uses width = height = 4,
+ * fov = 3, up = (0, 1, 0), light = normalize(0, -1, 1) and background (128, 128, 128). */
+typedef struct {
+  float origin[3];
+  float direction[3];
+  float up[3];
+  float width, height, fov;
+  float light[3];
+  uint32_t background; /* 0xRRGGBBAA */
+} svo_viewport;
+/* Ray generation, cast and shading in one kernel: W x H pixels, 4 bytes (r, g, b, a) each,
+ * row-major from the top row (the example's `viewport_size_height - y - 1`), into device memory
+ * `rgba`.  Pixels where the example panics (a hit without albedo) or loops forever (work cap)
+ * are written as (0, 0, 0, 0) and counted into the optional device counter *unshaded (added to,
+ * not reset).  Allocates nothing; rays never touch memory. */
+svo_status svo_render_viewport(svo_scene* scene, const svo_viewport* viewport, uint32_t width_px, uint32_t height_px,
+                               uint8_t* rgba, unsigned long long* unshaded, void* stream);
 
 /* ---- batched multi-scene cast (one persistent launch) ------------------ */
 typedef struct {

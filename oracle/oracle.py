@@ -22,6 +22,19 @@ OP_DTYPE = np.dtype([("x", "<u2"), ("y", "<u2"), ("z", "<u2"), ("op", "u1"), ("k
 assert OP_DTYPE.itemsize == 20
 
 
+class Viewport(ctypes.Structure):
+    _fields_ = [("origin", ctypes.c_float * 3), ("direction", ctypes.c_float * 3), ("up", ctypes.c_float * 3),
+                ("width", ctypes.c_float), ("height", ctypes.c_float), ("fov", ctypes.c_float),
+                ("light", ctypes.c_float * 3), ("background", ctypes.c_uint32)]
+
+
+def viewport_struct(vp):
+    """vp: dict with origin, direction, up, width, height, fov, light (3-sequences / floats), background."""
+    f3 = ctypes.c_float * 3
+    return Viewport(f3(*vp["origin"]), f3(*vp["direction"]), f3(*vp["up"]), vp["width"], vp["height"], vp["fov"],
+                    f3(*vp["light"]), vp["background"])
+
+
 class Hits(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in (
         "status", "brick_octant", "entry_kind", "node_key", "voxel_index", "pix", "albedo", "user",
@@ -62,6 +75,7 @@ def lib():
         L.orc_apply_ops.argtypes = [vp, vp, u64, ctypes.POINTER(u64)]
         L.orc_get.argtypes = [vp, u32, u32, u32, ctypes.POINTER(u32)]
         L.orc_cast.argtypes = [vp, u64, vp, vp, vp, vp, vp, vp, ctypes.POINTER(Hits), i]
+        L.orc_render_viewport.argtypes = [vp, ctypes.POINTER(Viewport), u32, u32, vp, ctypes.POINTER(u64), i]
         L.orc_node_count.argtypes = [vp]
         L.orc_node_count.restype = u64
         L.orc_node_record.argtypes = [vp, u64, ctypes.POINTER(u64)]
@@ -175,6 +189,16 @@ class Tree:
         if rc != OK:
             raise OracleError(rc, "cast")
         return out
+
+    def render_viewport(self, vp, width, height, threads=1):
+        """One frame of examples/cpu_render.rs.  Returns (rgba (height, width, 4) uint8, unshaded pixel count)."""
+        img = np.zeros((height, width, 4), dtype=np.uint8)
+        bad = ctypes.c_uint64(0)
+        rc = lib().orc_render_viewport(self._h, ctypes.byref(viewport_struct(vp)), width, height, img.ctypes.data,
+                                       ctypes.byref(bad), threads)
+        if rc != OK:
+            raise OracleError(rc, "render_viewport")
+        return img, bad.value
 
     def cast_one(self, origin, direction):
         r = self.cast([origin], [direction])

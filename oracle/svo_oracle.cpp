@@ -18,6 +18,7 @@
 #include <cstdint>
 #include <cstring>
 #include <stdexcept>
+#include <atomic>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -1864,6 +1865,73 @@ int orc_cast(void* tree, uint64_t n, const float* ox, const float* oy, const flo
     pool.emplace_back(work, b, e);
   }
   for (auto& th : pool) th.join();
+  return ORC_OK;
+}
+
+// examples/cpu_render.rs:77-138 (one iteration of its render loop; the viewport, light and
+// background are parameters instead of the example's constants)
+static inline V3f cross(V3f a, V3f b) {  // vector.rs:186-192
+  return V3f{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+static inline float dot(V3f a, V3f b) { return a.x * b.x + a.y * b.y + a.z * b.z; }  // vector.rs:182-184
+static inline uint8_t as_u8(float v) {  // `f32 as u8`: truncate, saturate, NaN -> 0
+  if (!(v > 0.0f)) return 0;
+  if (v >= 255.0f) return 255;
+  return (uint8_t)v;
+}
+
+int orc_render_viewport(void* tree, const orc_viewport* vp, uint32_t W, uint32_t H, uint8_t* rgba,
+                        uint64_t* unshaded, int threads) {
+  const Octree* t = static_cast<const Octree*>(tree);
+  if (!t || !vp || !rgba) return ORC_ERR_ARGUMENT;
+  const V3f origin{vp->origin[0], vp->origin[1], vp->origin[2]};
+  const V3f dir{vp->direction[0], vp->direction[1], vp->direction[2]};
+  const V3f up{vp->up[0], vp->up[1], vp->up[2]};
+  const V3f light{vp->light[0], vp->light[1], vp->light[2]};
+  const V3f right = normalized(cross(up, dir));
+  const float pixel_width = vp->width / (float)W, pixel_height = vp->height / (float)H;
+  const V3f bottom_left = origin + dir * vp->fov - up * (vp->height / 2.0f) - right * (vp->width / 2.0f);
+  std::atomic<uint64_t> bad{0};
+  auto work = [&](uint32_t x0, uint32_t x1) {
+    uint64_t local = 0;
+    for (uint32_t x = x0; x < x1; ++x)
+      for (uint32_t y = 0; y < H; ++y) {
+        const V3f glass = bottom_left + right * (float)x * pixel_width + up * (float)y * pixel_height;
+        const Ray ray{origin, normalized(glass - origin)};
+        const Octree::CastResult h = t->get_by_ray(ray);
+        uint8_t* px = rgba + 4 * ((size_t)(H - y - 1) * W + x);
+        if (h.status == 0) {
+          px[0] = (uint8_t)(vp->background >> 24);
+          px[1] = (uint8_t)(vp->background >> 16);
+          px[2] = (uint8_t)(vp->background >> 8);
+          px[3] = (uint8_t)vp->background;
+        } else if (h.status == 1 && (h.entry.kind & 1u)) {
+          const float strength = 1.0f - (dot(h.normal, light) / 2.0f + 0.5f);
+          const uint32_t a = h.entry.rgba;
+          px[0] = as_u8((float)(uint8_t)(a >> 24) * strength);
+          px[1] = as_u8((float)(uint8_t)(a >> 16) * strength);
+          px[2] = as_u8((float)(uint8_t)(a >> 8) * strength);
+          px[3] = 255;
+        } else {
+          px[0] = px[1] = px[2] = px[3] = 0;
+          ++local;
+        }
+      }
+    bad += local;
+  };
+  if (threads <= 1 || (uint64_t)W * H < 4096) {
+    work(0, W);
+  } else {
+    std::vector<std::thread> pool;
+    const uint32_t chunk = (W + threads - 1) / threads;
+    for (int k = 0; k < threads; ++k) {
+      const uint32_t b = (uint32_t)k * chunk, e = std::min(W, b + chunk);
+      if (b >= e) break;
+      pool.emplace_back(work, b, e);
+    }
+    for (auto& th : pool) th.join();
+  }
+  if (unshaded) *unshaded = bad.load();
   return ORC_OK;
 }
 

@@ -79,6 +79,21 @@ int orc_cast(void* tree, uint64_t n, const float* ox, const float* oy, const flo
              const float* dy, const float* dz, const orc_hits* out, int threads);
 
 /* Structure inspection (canonical per-node records, palettes). */
+/* One frame of examples/cpu_render.rs: a viewport of width x height world units at distance fov
+   in front of origin along direction, pixels spread from its bottom-left corner along right =
+   normalize(up x direction) and up, one ray per pixel from origin, diffuse shading against light. */
+typedef struct {
+  float origin[3], direction[3], up[3];
+  float width, height, fov;
+  float light[3];
+  uint32_t background; /* 0xRRGGBBAA of a pixel whose ray hits nothing */
+} orc_viewport;
+/* rgba: 4 bytes (r, g, b, a) per pixel, row-major from the top row.  A hit whose entry has no
+   albedo (where the example's unwrap() panics) or a ray that reaches the work cap is stored as
+   (0, 0, 0, 0) and counted in *unshaded (may be NULL). */
+int orc_render_viewport(void* tree, const orc_viewport* vp, uint32_t width_px, uint32_t height_px, uint8_t* rgba,
+                        uint64_t* unshaded, int threads);
+
 uint64_t orc_node_count(void* tree);
 int orc_node_record(void* tree, uint64_t key, uint64_t rec[40]);
 uint64_t orc_palette(void* tree, int which, uint32_t* out, uint64_t max);

@@ -13,10 +13,10 @@ import ctypes
 import numpy as np
 
 from ._lib import (HIT_FIELDS, OP_DTYPE, Hits, LaunchConfig, Rays, Request, RequestResult, SceneRecipe, ServerConfig,
-                   ServerStats, check, lib)
+                   ServerStats, Viewport, check, lib)
 
 __all__ = ["Octree", "OctreeError", "OP_DTYPE", "HIT_FIELDS", "gen_scene", "gen_camera_rays", "gen_sphere_rays",
-           "SceneRecipe", "LaunchConfig", "BatchWorkspace", "Server", "lib"]
+           "SceneRecipe", "LaunchConfig", "BatchWorkspace", "Server", "viewport", "orbit_viewport", "lib"]
 
 OK, INVALID_SIZE, INVALID_BRICK_DIM, INVALID_STRUCTURE, INVALID_POSITION = 0, 1, 2, 3, 4
 
@@ -158,6 +158,13 @@ class Octree:
         h = Hits(**{k: _vp(out[k].ctypes.data) if k in out else None for k in HIT_FIELDS})
         check(lib().svo_cast_host(self._h, ctypes.byref(r), n, ctypes.byref(h), _vp(stream)))
 
+    def render_viewport(self, viewport, width, height, rgba, unshaded=0, stream=0):
+        """Fused render of examples/cpu_render.rs's frame into device memory: `viewport` from
+        viewport(), `rgba` a device pointer to height * width * 4 bytes (row-major from the top
+        row), `unshaded` an optional device pointer to a u64 counter."""
+        check(lib().svo_render_viewport(self._h, ctypes.byref(viewport), width, height, _vp(rgba), _vp(unshaded),
+                                        _vp(stream)))
+
     def get_by_ray(self, origin, direction):
         """Octree::get_by_ray for one ray: None or ((kind, rgba, user), point, normal)."""
         r = self.cast_host([origin], [direction])
@@ -165,6 +172,32 @@ class Octree:
             return None
         return ((int(r["entry_kind"][0]), int(r["albedo"][0]), int(r["user"][0])),
                 (r["px"][0], r["py"][0], r["pz"][0]), (r["nx"][0], r["ny"][0], r["nz"][0]))
+
+
+def _normalized(v):
+    """V3c::normalized (vector.rs:75-81) in f32."""
+    v = np.asarray(v, dtype=np.float32)
+    n = np.sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2], dtype=np.float32)
+    return v / n
+
+
+def viewport(origin, direction, up=(0.0, 1.0, 0.0), width=4.0, height=4.0, fov=3.0, light=None,
+             background=0x808080FF):
+    """The viewport of examples/cpu_render.rs (its constants are the defaults; light defaults to
+    normalize(0, -1, 1)).  `direction` is used as given: the example passes a unit vector."""
+    f3 = ctypes.c_float * 3
+    if light is None:
+        light = _normalized([0.0, -1.0, 1.0])
+    return Viewport(f3(*map(float, origin)), f3(*map(float, direction)), f3(*map(float, up)), width, height, fov,
+                    f3(*map(float, light)), background)
+
+
+def orbit_viewport(angle, radius, **kw):
+    """The example's camera: origin (sin(angle) r, r, cos(angle) r) looking at the world origin."""
+    a = np.float32(angle)
+    r = np.float32(radius)
+    origin = np.array([np.sin(a) * r, r, np.cos(a) * r], dtype=np.float32)
+    return viewport(origin, _normalized(np.zeros(3, np.float32) - origin), **kw)
 
 
 class BatchWorkspace:

@@ -33,6 +33,12 @@ class Hits(ctypes.Structure):
     _fields_ = [(k, ctypes.c_void_p) for k in HIT_FIELDS]
 
 
+class Viewport(ctypes.Structure):
+    _fields_ = [("origin", ctypes.c_float * 3), ("direction", ctypes.c_float * 3), ("up", ctypes.c_float * 3),
+                ("width", ctypes.c_float), ("height", ctypes.c_float), ("fov", ctypes.c_float),
+                ("light", ctypes.c_float * 3), ("background", ctypes.c_uint32)]
+
+
 class SceneStats(ctypes.Structure):
     _fields_ = [("nodes", ctypes.c_uint64), ("reserved_nodes", ctypes.c_uint64), ("parted_bricks", ctypes.c_uint64),
                 ("colors", ctypes.c_uint64), ("datas", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64),
@@ -100,6 +106,7 @@ SIGNATURES = {
     "svo_scene_release_device": (_I32, [_VP]),
     "svo_cast": (_I32, [_VP, _P(Rays), _U64, _P(Hits), _VP]),
     "svo_cast_host": (_I32, [_VP, _P(Rays), _U64, _P(Hits), _VP]),
+    "svo_render_viewport": (_I32, [_VP, _P(Viewport), _U32, _U32, _VP, _VP, _VP]),
     "svo_batch_workspace_create": (_I32, [_P(_VP)]),
     "svo_batch_workspace_destroy": (None, [_VP]),
     "svo_cast_batched": (_I32, [_VP, _P(BatchItem), _U32, _P(LaunchConfig), _VP]),

@@ -760,27 +760,34 @@ __host__ __device__ inline HitsView hits_view_of(const svo_hits& h) {
   return v;
 }
 
-__device__ __forceinline__ void write_hit(const SceneView& s, const HitsView& o, uint64_t i, HitRecord& h) {
-  uint32_t kind = 0, albedo = 0, user = 0;
-  if (h.status == 1) {  // pix_get_ref (src/octree/node.rs:381-419)
-    const uint32_t c = h.pix & 0xFFFFu, d = h.pix >> 16;
-    if (c < 0xFFFFu) {
-      if (c >= s.n_colors) {
-        h.status = 3;
-      } else {
-        kind |= 1u;
-        albedo = __ldg(s.colors + c);
-      }
-    }
-    if (d != 0xFFFFu) {
-      if (d >= s.n_datas) {
-        h.status = 3;
-      } else {
-        kind |= 2u;
-        user = __ldg(s.datas + d);
-      }
+// pix_get_ref (src/octree/node.rs:381-419): the hit's entry kind and payload from its palette
+// indices; an index past a palette panics in the reference (status 3).
+__device__ __forceinline__ void resolve_entry(const SceneView& s, HitRecord& h, uint32_t& kind, uint32_t& albedo,
+                                              uint32_t& user) {
+  kind = albedo = user = 0;
+  if (h.status != 1) return;
+  const uint32_t c = h.pix & 0xFFFFu, d = h.pix >> 16;
+  if (c < 0xFFFFu) {
+    if (c >= s.n_colors) {
+      h.status = 3;
+    } else {
+      kind |= 1u;
+      albedo = __ldg(s.colors + c);
     }
   }
+  if (d != 0xFFFFu) {
+    if (d >= s.n_datas) {
+      h.status = 3;
+    } else {
+      kind |= 2u;
+      user = __ldg(s.datas + d);
+    }
+  }
+}
+
+__device__ __forceinline__ void write_hit(const SceneView& s, const HitsView& o, uint64_t i, HitRecord& h) {
+  uint32_t kind, albedo, user;
+  resolve_entry(s, h, kind, albedo, user);
   if (h.status != 1) {
     h.octant = h.node = h.pix = 0;
     h.voxel = 0xFFFFFFFFu;

@@ -9,9 +9,11 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "svo_cast.cuh"
+#include "svo_queue.h"
 
 namespace svo {
 
@@ -27,6 +29,61 @@ __global__ void __launch_bounds__(128, 7) cast_kernel(SceneView s, RaysView rays
                    __ldg(rays.dy + i), __ldg(rays.dz + i), h);
   write_hit(s, out, i, h);
   if (kCount) write_counters(out, i, h);
+}
+
+// Queued cast: a persistent grid whose warps claim 32 consecutive rays at a time from a work
+// counter.  The cost of a ray varies by orders of magnitude (a sky ray leaves after a few node
+// visits, a grazing ray walks a whole cave), and a warp that finishes early takes more work
+// instead of idling until its block's slowest warp is done.  The counter starts at 0.
+template <bool kCount>
+__global__ void __launch_bounds__(128, 7)
+    queue_kernel(SceneView s, RaysView rays, HitsView out, uint64_t n, unsigned long long* __restrict__ counter) {
+  __shared__ SharedLuts L;
+  fill_shared_luts(L);
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31u;
+  for (;;) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(counter, 32ull);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (base >= n) break;
+    const uint64_t i = base + lane;
+    if (i >= n) continue;
+    HitRecord h;
+    cast_one<kCount>(s, L, __ldg(rays.ox + i), __ldg(rays.oy + i), __ldg(rays.oz + i), __ldg(rays.dx + i),
+                     __ldg(rays.dy + i), __ldg(rays.dz + i), h);
+    write_hit(s, out, i, h);
+    if (kCount) write_counters(out, i, h);
+  }
+}
+
+constexpr uint64_t kQueueMinRays = 1u << 15;  // below this the one-thread-per-ray grid is as fast
+
+void destroy_queues(DeviceImage& d) {
+  if (!d.queues) return;
+  cudaFree(d.queues->counters);
+  delete d.queues;
+  d.queues = nullptr;
+}
+
+svo_status create_queues(DeviceImage& d) {
+  if (d.queues) return SVO_OK;
+  CastQueues* q = new CastQueues();
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&q->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q->blocks_per_sm, queue_kernel<false>, 128, 0);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q->blocks_per_sm_count, queue_kernel<true>, 128, 0);
+  if (e == cudaSuccess) e = cudaMalloc(&q->counters, kQueueSlots * sizeof(unsigned long long));
+  if (e != cudaSuccess) {
+    cudaFree(q->counters);
+    delete q;
+    return fail(e == cudaErrorMemoryAllocation ? SVO_ERR_OUT_OF_MEMORY : SVO_ERR_CUDA,
+                std::string("work counters: ") + cudaGetErrorString(e));
+  }
+  d.queues = q;
+  return SVO_OK;
 }
 
 int g_cast_mode = 0;
@@ -119,6 +176,10 @@ svo_status full_upload(svo_scene* sc, cudaStream_t st) {
   HostOctree& t = sc->tree;
   DeviceImage& d = sc->dev;
   free_device(d);
+  {
+    const svo_status qs = create_queues(d);
+    if (qs != SVO_OK) return qs;
+  }
   const uint64_t nn = t.nodes(), nb = std::max<uint64_t>(1, t.arena.slots());
   const uint64_t nc = std::max<uint64_t>(1, t.colors.size()), ndt = std::max<uint64_t>(1, t.datas.size());
   // headroom so that later in-place syncs rarely need a new allocation
@@ -238,6 +299,21 @@ svo_status launch_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const sv
   const HitsView hv = hits_view_of(*hits);
   const bool count = counts_requested(*hits);
   const unsigned block = 128;
+  CastQueues* q = sc->dev.queues;
+  if (q && n >= kQueueMinRays) {
+    std::lock_guard<std::mutex> lock(q->m);
+    if (unsigned long long* ctr = queue_counter(q, st)) {
+      const int per_sm = std::max(1, count ? q->blocks_per_sm_count : q->blocks_per_sm);
+      const uint64_t grid = std::min<uint64_t>((uint64_t)q->sm_count * per_sm, (n + block - 1) / block);
+      SVO_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st));
+      if (count)
+        queue_kernel<true><<<(unsigned)grid, block, 0, st>>>(v, rv, hv, n, ctr);
+      else
+        queue_kernel<false><<<(unsigned)grid, block, 0, st>>>(v, rv, hv, n, ctr);
+      SVO_CUDA_TRY(cudaGetLastError());
+      return SVO_OK;
+    }
+  }
   const uint64_t grid = (n + block - 1) / block;
   if (grid > 0x7FFFFFFFull) return fail(SVO_ERR_ARGUMENT, "svo_cast: too many rays for one launch");
   if (count)
@@ -388,6 +464,7 @@ svo_status svo_scene_release_device(svo_scene* sc) {
   if (!sc) return fail(SVO_ERR_ARGUMENT, "NULL scene");
   destroy_pipeline(sc->dev);
   free_device(sc->dev);
+  destroy_queues(sc->dev);
   std::fill(sc->tree.node_dirty.begin(), sc->tree.node_dirty.end(), 1);
   std::fill(sc->tree.arena.dirty().begin(), sc->tree.arena.dirty().end(), 1);
   return SVO_OK;
@@ -397,6 +474,7 @@ void svo_scene_destroy(svo_scene* sc) {
   if (!sc) return;
   destroy_pipeline(sc->dev);
   free_device(sc->dev);
+  destroy_queues(sc->dev);
   delete sc;
 }
 

@@ -51,6 +51,8 @@ struct SceneView {
 // Cast form selected by svo_set_cast_mode (0 automatic, 1 literal only).
 extern int g_cast_mode;
 
+struct CastQueues;  // work counters of the queued cast (svo_device.cu)
+
 struct DeviceImage {
   DevNode* nodes = nullptr;
   uint32_t* voxels = nullptr;
@@ -66,6 +68,8 @@ struct DeviceImage {
   // workspace of svo_cast_host (device buffers, grown on demand)
   void* ws = nullptr;
   uint64_t ws_bytes = 0;
+  // one work counter per stream that casts this scene; kept across re-uploads
+  CastQueues* queues = nullptr;
 };
 
 }  // namespace svo

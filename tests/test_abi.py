@@ -8,6 +8,7 @@ import shocovox_gb300 as svo
 from shocovox_gb300 import _lib
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INCLUDE = os.path.join(ROOT, "include")
 
 
 def declared_functions():
@@ -65,3 +66,34 @@ def test_generators_are_deterministic():
     assert abs(n - 1).max() < 1e-6
     o2, d2 = svo.gen_sphere_rays([8, 8, 8], 13.0, 1000, 7)
     assert abs(((o2 - 8) ** 2).sum(1) ** 0.5 - 13).max() < 1e-3
+
+
+def test_struct_layouts_match_bindings(tmp_path):
+    """Every struct of svo.h has the size and field offsets of its ctypes mirror."""
+    from shocovox_gb300 import _lib as L
+    pairs = {"svo_rays": L.Rays, "svo_hits": L.Hits, "svo_viewport": L.Viewport, "svo_scene_stats": L.SceneStats,
+             "svo_scene_recipe": L.SceneRecipe, "svo_launch_config": L.LaunchConfig,
+             "svo_server_config": L.ServerConfig, "svo_request": L.Request, "svo_request_result": L.RequestResult,
+             "svo_server_stats": L.ServerStats, "svo_batch_item": L.BatchItem}
+    c_fields = {
+        "svo_hits": [f for f, _ in L.Hits._fields_], "svo_rays": [f for f, _ in L.Rays._fields_],
+        "svo_viewport": [f for f, _ in L.Viewport._fields_],
+    }
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "svo.h"', 'int main(void) {']
+    for name in pairs:
+        lines.append('  printf("%s %%zu\\n", sizeof(%s));' % (name, name))
+    for name, fields in c_fields.items():
+        for f in fields:
+            lines.append('  printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (name, f, name, f))
+    lines.append('  return 0;\n}')
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", INCLUDE, str(src), "-o", str(exe)], check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines())
+    for name, cls in pairs.items():
+        assert int(got[name]) == ctypes.sizeof(cls), name
+    for name, fields in c_fields.items():
+        cls = pairs[name]
+        for f in fields:
+            assert int(got["%s.%s" % (name, f)]) == getattr(cls, f).offset, (name, f)
