@@ -93,12 +93,12 @@ def measured_peak():
 
 
 def profile_traffic(workload):
-    """DRAM bytes per cast launch from the committed ncu summary of this workload, if any."""
+    """The committed ncu summary of this workload's cast launch (DRAM and L2 bytes per launch), if any."""
     p = os.path.join(ROOT, "profiles", "cast_%s_traffic.json" % workload)
     if os.path.exists(p):
         with open(p) as f:
-            return json.load(f).get("dram_bytes_per_launch")
-    return None
+            return json.load(f)
+    return {}
 
 
 class ClockSampler:
@@ -332,7 +332,7 @@ def run_multiscene(args, w):
     same = all(torch.equal(a[k], b[k]) for a, b in zip(ref_out, outs) for k in OUT_FIELDS)
     # one persistent launch captured in a CUDA graph (workspace already sized, blocks per SM fixed)
     if cfg.blocks_per_sm == 0:
-        per_sm = {64: 12, 96: 8, 128: 6}.get(cfg.block, 2)  # resident blocks at 80 registers per thread
+        per_sm = {64: 14, 96: 9, 128: 7}.get(cfg.block, 2)  # resident blocks at 72 registers per thread
         gcfg = svo.LaunchConfig(cfg.block, cfg.rays_per_chunk, per_sm, 0)
     else:
         gcfg = cfg
@@ -609,6 +609,21 @@ def run_viewport(args, w):
     e1.record(stream)
     torch.cuda.synchronize()
     cast_ms = e0.elapsed_time(e1) / args.steps
+    # the same rays cast one frame per launch, as the render launches
+    per = W * H
+
+    def cast_frames():
+        for k in range(len(vps)):
+            scene.cast({kk: v + 4 * k * per for kk, v in rp.items()},
+                       {kk: v + (1 if kk == "status" else 4) * k * per for kk, v in hp.items()}, per, s)
+    cast_frames()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        cast_frames()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    cast_frames_ms = e0.elapsed_time(e1) / args.steps
     cnt = {k: torch.empty(n, dtype=torch.int32, device=dev) for k in COUNTERS}
     st = torch.empty(n, dtype=torch.uint8, device=dev)
     scene.cast(rp, dict(status=st.data_ptr(), **{k: v.data_ptr() for k, v in cnt.items()}), n, s)
@@ -642,7 +657,11 @@ def run_viewport(args, w):
                    "build_s": round(build_s, 1), "unshaded_pixels": int(bad.item()),
                    "l2": "frames %.0f MB per step (larger than L2); the scene image stays resident" % (n * 4 / 1e6),
                    "cast_of_same_rays": {"value": round(n / (cast_ms / 1e3) / 1e6, 3), "ms_per_step": round(cast_ms, 4),
-                                         "note": "svo_cast, rays resident in HBM, status+albedo+normal out"}},
+                                         "note": "svo_cast, rays resident in HBM, status+albedo+normal out, "
+                                                 "all frames in one launch"},
+                   "cast_of_same_rays_per_frame": {"value": round(n / (cast_frames_ms / 1e3) / 1e6, 3),
+                                                   "ms_per_step": round(cast_frames_ms, 4),
+                                                   "note": "the same, one launch per frame like the render"}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_src,
                      "alg_bytes_per_launch": alg // len(vps), "alg_bytes_per_ray": round(alg / n, 2)},
@@ -822,7 +841,15 @@ def main():
 
     peak, peak_src = measured_peak()
     achieved = alg_bytes / (ms_step / 1e3) / 1e9
-    traffic = profile_traffic(args.workload)
+    prof = profile_traffic(args.workload)
+    traffic = prof.get("dram_bytes_per_launch")
+    l2 = None
+    if prof.get("l2_bytes_per_launch"):
+        l2 = {"bytes_per_launch": prof["l2_bytes_per_launch"],
+              "gbs": round(prof["l2_bytes_per_launch"] / (ms_step / 1e3) / 1e9, 1),
+              "hit_rate_pct": prof.get("l2_hit_rate_pct"), "l1_hit_rate_pct": prof.get("l1_hit_rate_pct"),
+              "frac_of_l2_peak": round(prof["l2_throughput_pct_of_peak"] / 100.0, 4),
+              "source": "ncu capture of one launch (profiles/); gbs with this run's kernel time"}
     if rank == 0:
         st = scene.stats()
         print(json.dumps({
@@ -841,7 +868,7 @@ def main():
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_src,
                          "alg_bytes_per_launch": alg_bytes,
-                         "alg_bytes_per_ray": round(alg_bytes / n, 2)},
+                         "alg_bytes_per_ray": round(alg_bytes / n, 2), "l2": l2},
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": n * 24,
                     "d2h_bytes_per_step": n * sum(OUT_BYTES.values())},

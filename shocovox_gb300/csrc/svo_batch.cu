@@ -31,12 +31,12 @@ struct BatchItemDev {
 
 constexpr uint32_t kMaxSharedItems = 1024;  // prefix sums staged in shared memory
 
-// At most kBatchMaxBlock threads per block with 6 resident blocks per SM (80 registers, a few
+// At most kBatchMaxBlock threads per block with 7 resident blocks per SM (72 registers, a few
 // spilled bytes); the launch configuration is checked against the block limit.
 constexpr uint32_t kBatchMaxBlock = 128;
 
 template <bool kCount>
-__global__ void __launch_bounds__(kBatchMaxBlock, 6)
+__global__ void __launch_bounds__(kBatchMaxBlock, 7)
     batched_kernel(const BatchItemDev* __restrict__ items, uint32_t n_items, uint64_t total,
                    unsigned long long* __restrict__ counter, uint32_t chunk) {
   __shared__ uint64_t s_begin[kMaxSharedItems];

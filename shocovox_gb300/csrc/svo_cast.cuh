@@ -410,6 +410,15 @@ struct RestartRun {
   float x, y, z;
   uint32_t k;
 };
+static __device__ __noinline__ RestartRun restart_exit(float x, float y, float z, float cx, float cy, float cz,
+                                                       float S, uint32_t n_max) {
+  RestartRun o;
+  o.k = restart_exit_run(x, y, z, cx, cy, cz, S, n_max);
+  o.x = x;
+  o.y = y;
+  o.z = z;
+  return o;
+}
 static __device__ __noinline__ RestartRun restart_run(float x, float y, float z, float cx, float cy, float cz, uint32_t flat,
                                                       float w, uint32_t n_max) {
   RestartRun o;
@@ -530,16 +539,22 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
   h.px = h.py = h.pz = h.nx = h.ny = h.nz = 0.0f;
   if (kCount) h.visits = h.creads = h.vreads = h.runs = 0;
 
+  // A ray whose origin lies outside the octree on some axis and that moves further away on it has
+  // both of that axis' slab distances negative, so tmax < 0 and the slab test below rejects it.
+  // The quotients are strictly negative when the origin is finite, at least 2^-100 below 0 (or
+  // above S) and the direction component at most 2^20 in size: no quotient rounds to -0.
+  {
+    const float S = s.size, lo = -0x1p-100f, big = 0x1p20f;
+    const bool fin = isfinite(ox) && isfinite(oy) && isfinite(oz) && fabsf(dx) <= big && fabsf(dy) <= big &&
+                     fabsf(dz) <= big;
+    if (fin && ((ox < lo && dx < 0.0f) || (ox > S && dx > 0.0f) || (oy < lo && dy < 0.0f) || (oy > S && dy > 0.0f) ||
+                (oz < lo && dz < 0.0f) || (oz > S && dz > 0.0f)))
+      return;
+  }
   FastRay r;
   r.dx = dx;
   r.dy = dy;
   r.dz = dz;
-  {  // get_dda_scale_factors (:99-112); powf(q, 2.) == q * q
-    const float a = dz / dx, b = dy / dx, c = dx / dy, d = dz / dy, e = dx / dz, f = dy / dz;
-    r.fx = sqrtf((1.0f + a * a) + b * b);
-    r.fy = sqrtf((c * c + 1.0f) + d * d);
-    r.fz = sqrtf((e * e + 1.0f) + f * f);
-  }
   // signum(d) > 0 <=> d > 0 or d == +0
   r.pos = (rsignum(dx) > 0.0f ? 1u : 0u) | (rsignum(dz) > 0.0f ? 2u : 0u) | (rsignum(dy) > 0.0f ? 4u : 0u);
   const float g4x = (r.pos & 1u) ? 4.0f : -4.0f, g4y = (r.pos & 4u) ? 4.0f : -4.0f, g4z = (r.pos & 2u) ? 4.0f : -4.0f;
@@ -560,6 +575,13 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
     r.py = oy + dy * t;
     r.pz = oz + dz * t;
     target = hash_region(r.px - 0.0f, r.py - 0.0f, r.pz - 0.0f, S * 0.5f);
+  }
+  {  // get_dda_scale_factors (:99-112), a function of the direction only, so formed after the
+     // root's slab test has let the ray in; powf(q, 2.) == q * q
+    const float a = dz / dx, b = dy / dx, c = dx / dy, d = dz / dy, e = dx / dz, f = dy / dz;
+    r.fx = sqrtf((1.0f + a * a) + b * b);
+    r.fy = sqrtf((c * c + 1.0f) + d * d);
+    r.fz = sqrtf((e * e + 1.0f) + f * f);
   }
   uint32_t work = 0;
   while (target != kOob) {
@@ -690,6 +712,28 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
         return;
       }
       if (kCount) h.visits++;
+      // When every axis moves the way the direction octant of the LUT says (only a negative
+      // component so small that 1 + d rounds to 1 breaks this), every later cell lies inside this
+      // cell's box towards the far corner, whose occupancy bits are empty: all later root tests fail
+      // and the ray leaves the octree without a hit.  Without counters only the work cap matters:
+      // an axis with |c| >= 2^-22 S advances by at least 3|c|/4 per restart (|c| >= 2 ulp), so at
+      // most S / (|c| / 2) + 2 restarts remain.  The counted cast takes the run to the exit exactly.
+      if (!((dx < 0.0f && 1.0f + dx >= 1.0f) || (dy < 0.0f && 1.0f + dy >= 1.0f) || (dz < 0.0f && 1.0f + dz >= 1.0f))) {
+        if (!kCount) {
+          const float cmax = fmaxf(fmaxf(fabsf(c01x), fabsf(c01y)), fabsf(c01z));
+          if (cmax >= S * 0x1p-22f && (float)work + S / (0.5f * cmax) + 2.0f < (float)kWorkCap) return;
+        }
+        const RestartRun run = restart_exit(r.px, r.py, r.pz, c01x, c01y, c01z, S, kWorkCap - work + 2u);
+        if (run.k == kRunNever) {
+          h.status = 2;
+          return;
+        }
+        if (kCount) {
+          h.visits += run.k - 1u;
+          h.runs += run.k - 1u;
+        }
+        return;
+      }
       // the visits before the next cell change fail alike; the cap holds if they fit in it
       const RestartRun run = restart_run(r.px, r.py, r.pz, c01x, c01y, c01z, flat, S * 0.25f, kWorkCap - work + 2u);
       const uint32_t k = run.k;

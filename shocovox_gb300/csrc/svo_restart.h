@@ -103,15 +103,12 @@ SVO_HD uint32_t nudge_run(float& p, float c, float lo, float hi, uint32_t n_max)
   return k;
 }
 
-// Number of restarts k >= 1 after which the point (x, y, z) -- inside the octree, in root bitmap
-// cell `flat` (x + 4 y + 16 z) -- first lies in another cell or outside the octree, moving it by
-// (cx, cy, cz) per restart to its value after those k restarts.  Returns kRunNever (the point is
-// left unchanged) when that takes n_max restarts or more, or never happens.  w = size / 4.
-SVO_HD uint32_t restart_cells_run(float& x, float& y, float& z, float cx, float cy, float cz, uint32_t flat,
-                                  float w, uint32_t n_max) {
-  const float lx = (float)(flat & 3u) * w, hx = (float)((flat & 3u) + 1u) * w;
-  const float ly = (float)((flat >> 2) & 3u) * w, hy = (float)(((flat >> 2) & 3u) + 1u) * w;
-  const float lz = (float)(flat >> 4) * w, hz = (float)((flat >> 4) + 1u) * w;
+// Number of restarts k >= 1 after which the point (x, y, z), inside the box [lx, hx) x [ly, hy) x
+// [lz, hz), first leaves it (see run_left), moving it by (cx, cy, cz) per restart to its value
+// after those k restarts.  Returns kRunNever (the point is left unchanged) when that takes n_max
+// restarts or more, or never happens.
+SVO_HD uint32_t restart_box_run(float& x, float& y, float& z, float cx, float cy, float cz, float lx, float hx,
+                                float ly, float hy, float lz, float hz, uint32_t n_max) {
   float ax = x, ay = y, az = z;
   const uint32_t kx = nudge_run(ax, cx, lx, hx, n_max);
   const uint32_t ky = nudge_run(ay, cy, ly, hy, n_max);
@@ -135,6 +132,21 @@ SVO_HD uint32_t restart_cells_run(float& x, float& y, float& z, float cx, float 
   y = ay;
   z = az;
   return k;
+}
+
+// The run until the point -- inside the octree, in root bitmap cell `flat` (x + 4 y + 16 z) --
+// lies in another cell or outside the octree.  w = size / 4.
+SVO_HD uint32_t restart_cells_run(float& x, float& y, float& z, float cx, float cy, float cz, uint32_t flat,
+                                  float w, uint32_t n_max) {
+  const float jx = (float)(flat & 3u), jy = (float)((flat >> 2) & 3u), jz = (float)(flat >> 4);
+  return restart_box_run(x, y, z, cx, cy, cz, jx * w, (jx + 1.0f) * w, jy * w, (jy + 1.0f) * w, jz * w,
+                         (jz + 1.0f) * w, n_max);
+}
+
+// The run until the point leaves the octree [0, S)^3.
+SVO_HD uint32_t restart_exit_run(float& x, float& y, float& z, float cx, float cy, float cz, float S,
+                                 uint32_t n_max) {
+  return restart_box_run(x, y, z, cx, cy, cz, 0.0f, S, 0.0f, S, 0.0f, S, n_max);
 }
 
 }  // namespace svo

@@ -154,6 +154,51 @@ int main(int argc, char** argv) {
       return 1;
     }
   }
+  // runs until the point leaves the octree
+  for (long i = 0; i < n_random / 4; ++i) {
+    const float s = sizes[next_u64() % 6];
+    const float x = (float)(uni() * s), y = (float)(uni() * s), zz = (float)(uni() * s);
+    if (!(x > 0.0f && y > 0.0f && zz > 0.0f)) continue;
+    float d[3] = {(float)(uni() * 2 - 1), (float)(uni() * 2 - 1), (float)(uni() * 2 - 1)};
+    const float nn = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    if (!(nn > 0.0f)) continue;
+    for (float& v : d) v /= nn;
+    if (next_u64() % 5 == 0) d[next_u64() % 3] = 0.0f;
+    if (next_u64() % 7 == 0) d[next_u64() % 3] *= 1e-6f;
+    const float cx = d[0] * 0.1f, cy = d[1] * 0.1f, cz = d[2] * 0.1f;
+    const uint32_t n_max = next_u64() % 3 == 0 ? 1u + (uint32_t)(next_u64() % 5000) : kBruteLimit;
+    float ax = x, ay = y, az = zz;
+    const uint32_t k = svo::restart_exit_run(ax, ay, az, cx, cy, cz, s, n_max);
+    float bx = x, by = y, bz = zz;
+    uint32_t kb = 0;
+    for (;;) {
+      if (kb >= n_max) {
+        kb = kRunNever;
+        break;
+      }
+      const float nx = bx + cx, ny = by + cy, nz = bz + cz;
+      if (nx == bx && ny == by && nz == bz) {
+        kb = kRunNever;
+        break;
+      }
+      ++kb;
+      bx = nx;
+      by = ny;
+      bz = nz;
+      if (!(bx < s && by < s && bz < s && bx > 0.0f && by > 0.0f && bz > 0.0f)) break;
+    }
+    ++cases;
+    if (kb != kRunNever && kb >= n_max) kb = kRunNever;
+    const bool same = kb == kRunNever ? (k == kRunNever && f32_bits(ax) == f32_bits(x) && f32_bits(ay) == f32_bits(y) &&
+                                         f32_bits(az) == f32_bits(zz))
+                                      : (k == kb && f32_bits(ax) == f32_bits(bx) && f32_bits(ay) == f32_bits(by) &&
+                                         f32_bits(az) == f32_bits(bz));
+    if (!same) {
+      printf("MISMATCH restart_exit_run s=%g p=(%a,%a,%a) c=(%a,%a,%a) n_max=%u: got k=%u, additions give k=%u\n", s, x,
+             y, zz, cx, cy, cz, n_max, k, kb);
+      return 1;
+    }
+  }
   printf("OK %ld cases\n", cases);
   return 0;
 }
