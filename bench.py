@@ -159,6 +159,16 @@ def alg_bytes_of(performed_visits, child_reads, voxel_reads, hits):
     return 12 * performed_visits + 4 * child_reads + 4 * voxel_reads + 8 * hits
 
 
+def max_over_ranks(seconds, pg):
+    """The slowest rank's time: the job is done when the last replica is (gloo all-reduce on the host)."""
+    if pg is None:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t[0])
+
+
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
@@ -799,10 +809,7 @@ def main():
     ms = e0.elapsed_time(e1)
     if pg:
         pg.barrier()
-    if pg:
-        t = torch.tensor([ms], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t[0])
+    ms = max_over_ranks(ms, pg)
     ms_step = ms / args.steps
     value = n * world / (ms_step / 1e3) / 1e6
 
@@ -823,11 +830,7 @@ def main():
     t0 = time.perf_counter()
     for _ in range(args.steps):
         scene.cast_host_soa(cols_np, out_np, s)
-    e2e_s = time.perf_counter() - t0
-    if pg:
-        t = torch.tensor([e2e_s], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_s = float(t[0])
+    e2e_s = max_over_ranks(time.perf_counter() - t0, pg)
     e2e_value = n * world * args.steps / e2e_s / 1e6
 
     cpu = None
