@@ -75,6 +75,13 @@ def lib():
         L.orc_apply_ops.argtypes = [vp, vp, u64, ctypes.POINTER(u64)]
         L.orc_get.argtypes = [vp, u32, u32, u32, ctypes.POINTER(u32)]
         L.orc_cast.argtypes = [vp, u64, vp, vp, vp, vp, vp, vp, ctypes.POINTER(Hits), i]
+        L.orc_cast_lod.argtypes = [vp, u64, vp, vp, vp, vp, vp, vp, ctypes.c_float, ctypes.POINTER(Hits), i]
+        L.orc_mip_switch.argtypes = [vp, i]
+        L.orc_mip_set_method.argtypes = [vp, u32, u32, ctypes.c_float]
+        L.orc_mip_set_color_threshold.argtypes = [vp, u32, ctypes.c_float]
+        L.orc_mip_recalculate.argtypes = [vp]
+        L.orc_mip_sample_root.argtypes = [vp, u32, u32, u32, u32, ctypes.POINTER(u32)]
+        L.orc_node_mip.argtypes = [vp, u64, ctypes.POINTER(u32), vp]
         L.orc_render_viewport.argtypes = [vp, ctypes.POINTER(Viewport), u32, u32, vp, ctypes.POINTER(u64), i]
         L.orc_node_count.argtypes = [vp]
         L.orc_node_count.restype = u64
@@ -177,15 +184,19 @@ class Tree:
             raise OracleError(rc, "get")
         return tuple(out)  # (kind, rgba, user)
 
-    def cast(self, origins, directions, threads=1):
-        """origins/directions: (n,3) float32.  Returns a dict of per-ray numpy arrays."""
+    def cast(self, origins, directions, threads=1, viewing_distance=None):
+        """origins/directions: (n,3) float32.  Returns a dict of per-ray numpy arrays.  With a viewing
+        distance the cast is get_by_ray_at_lod."""
         o = f32arr(origins).reshape(-1, 3)
         d = f32arr(directions).reshape(-1, 3)
         n = o.shape[0]
         cols = [np.ascontiguousarray(o[:, k]) for k in range(3)] + [np.ascontiguousarray(d[:, k]) for k in range(3)]
         out = {k: np.zeros(n, dtype=t) for k, t in HIT_FIELDS.items()}
         h = Hits(**{k: out[k].ctypes.data for k in HIT_FIELDS})
-        rc = lib().orc_cast(self._h, n, *[_ptr(c) for c in cols], ctypes.byref(h), threads)
+        if viewing_distance is None:
+            rc = lib().orc_cast(self._h, n, *[_ptr(c) for c in cols], ctypes.byref(h), threads)
+        else:
+            rc = lib().orc_cast_lod(self._h, n, *[_ptr(c) for c in cols], viewing_distance, ctypes.byref(h), threads)
         if rc != OK:
             raise OracleError(rc, "cast")
         return out
@@ -199,6 +210,37 @@ class Tree:
         if rc != OK:
             raise OracleError(rc, "render_viewport")
         return img, bad.value
+
+    # ---- MIP maps (octree/mipmap.rs) ----
+    BOX, POINT, POINT_BD, POSTERIZE, POSTERIZE_BD = range(5)
+
+    def mip_switch(self, enabled):
+        self._check(lib().orc_mip_switch(self._h, int(bool(enabled))), "mip_switch")
+
+    def mip_set_method(self, level, method, thr=0.0):
+        self._check(lib().orc_mip_set_method(self._h, level, method, thr), "mip_set_method")
+
+    def mip_set_color_threshold(self, level, thr):
+        self._check(lib().orc_mip_set_color_threshold(self._h, level, thr), "mip_set_color_threshold")
+
+    def mip_recalculate(self):
+        self._check(lib().orc_mip_recalculate(self._h), "mip_recalculate")
+
+    def mip_sample_root(self, octant, pos):
+        out = (ctypes.c_uint32 * 3)()
+        self._check(lib().orc_mip_sample_root(self._h, octant, pos[0], pos[1], pos[2], out), "mip_sample_root")
+        return tuple(out)  # (kind, rgba, user)
+
+    def node_mip(self, key, brick_dim):
+        """(kind, values): kind 0 empty, 1 solid, 2 parted, 3 past node_mips."""
+        kind = ctypes.c_uint32(0)
+        vals = np.zeros(max(1, brick_dim ** 3), dtype=np.uint32)
+        self._check(lib().orc_node_mip(self._h, key, ctypes.byref(kind), vals.ctypes.data), "node_mip")
+        return kind.value, vals
+
+    def _check(self, rc, what):
+        if rc != OK:
+            raise OracleError(rc, what)
 
     def cast_one(self, origin, direction):
         r = self.cast([origin], [direction])

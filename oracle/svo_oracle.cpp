@@ -14,11 +14,13 @@
 #include "svo_oracle.h"
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <stdexcept>
 #include <atomic>
+#include <map>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -471,6 +473,30 @@ struct Octree {
   std::unordered_map<uint32_t, size_t> color_map, data_map;
   bool auto_simplify = true;
   int recursion = 0;
+  // MIP maps (types.rs:146-160, mipmap.rs:578-595): disabled by default
+  enum MipMethod : uint32_t { MIP_BOX = 0, MIP_POINT = 1, MIP_POINT_BD = 2, MIP_POSTERIZE = 3, MIP_POSTERIZE_BD = 4 };
+  struct MipSampler {
+    MipMethod method;
+    float thr;
+  };
+  bool mips_enabled = false;
+  std::map<size_t, MipSampler> mip_methods{
+      {1, {MIP_POINT, 0.0f}}, {2, {MIP_BOX, 0.0f}}, {3, {MIP_BOX, 0.0f}}, {4, {MIP_BOX, 0.0f}}};
+  std::map<size_t, float> mip_color_thr{{2, 0.1f}, {3, 0.05f}, {4, 0.02f}};
+  std::vector<BrickData> node_mips{BrickData{}};  // mod.rs:198
+  BrickData& mip(size_t key) {
+    if (key >= node_mips.size()) throw Panic("node_mips index out of bounds");
+    return node_mips[key];
+  }
+  const BrickData& mip(size_t key) const {
+    if (key >= node_mips.size()) throw Panic("node_mips index out of bounds");
+    return node_mips[key];
+  }
+  // `node_mips.resize(node_mips.len().max(nodes.len()), BrickData::Empty)`, which the reference
+  // does beside most node_children resizes
+  void mips_resize() {
+    if (node_mips.size() < nodes.len()) node_mips.resize(nodes.len());
+  }
 
   NodeChildren& nc(uint64_t key) {
     if (key >= node_children.size()) throw Panic("node_children index out of bounds");
@@ -741,6 +767,7 @@ struct Octree {
           if (octant == target_octant) {
             nn[octant] = (uint32_t)push_node(NodeContent{});
             nc_resize(std::max(node_children.size(), (size_t)nn[octant] + 1));
+            mips_resize();
           }
         } else if (brick.kind == B_SOLID) {
           NodeContent c;
@@ -748,6 +775,7 @@ struct Octree {
           c.bricks[0] = BrickData::Solid(brick.solid);
           nn[octant] = (uint32_t)push_node(std::move(c));
           nc_resize(std::max(node_children.size(), (size_t)nn[octant] + 1));
+          mips_resize();
           nc(nn[octant]) = NodeChildren::Bitmap(UINT64_MAX);
         } else {
           NodeContent c;
@@ -755,6 +783,7 @@ struct Octree {
           c.bricks[0] = BrickData::Parted(brick.parted);
           nn[octant] = (uint32_t)push_node(std::move(c));
           nc_resize(std::max(node_children.size(), (size_t)nn[octant] + 1));
+          mips_resize();
           // detail.rs:387-394: computed from bricks[octant], which was swapped out to Empty above
           nc(nn[octant]) = NodeChildren::Bitmap(calculate_occupied_bits(node_content.bricks[octant], brick_dim));
         }
@@ -764,6 +793,7 @@ struct Octree {
       if (brick.kind == B_EMPTY) {
         nn[target_octant] = (uint32_t)push_node(NodeContent{});
         nc_resize(std::max(node_children.size(), (size_t)nn[target_octant] + 1));
+        mips_resize();
         nc(nn[target_octant]) = NodeChildren::Bitmap(0);
       } else if (brick.kind == B_SOLID) {
         for (size_t octant = 0; octant < 8; ++octant) {
@@ -771,7 +801,7 @@ struct Octree {
           c.kind = C_UNIFORM;
           c.bricks[0] = BrickData::Solid(brick.solid);
           nn[octant] = (uint32_t)push_node(std::move(c));
-          nc_resize(std::max(node_children.size(), (size_t)nn[octant] + 1));
+          nc_resize(std::max(node_children.size(), (size_t)nn[octant] + 1));  // node_mips not resized (:439-446)
           nc(nn[octant]) = NodeChildren::Bitmap(UINT64_MAX);
         }
       } else {
@@ -783,6 +813,7 @@ struct Octree {
           c.bricks[0] = BrickData::Parted(std::move(children_bricks[octant]));
           nn[octant] = (uint32_t)push_node(std::move(c));
           nc_resize(std::max(node_children.size(), (size_t)nn[octant] + 1));
+          mips_resize();
           nc(nn[octant]) = NodeChildren::Bitmap(bits);
         }
       }
@@ -1219,6 +1250,7 @@ struct Octree {
           u.bricks[0] = BrickData::Solid(target_content);
           uint32_t nk = (uint32_t)push_node(std::move(u));
           nc_resize(std::max(node_children.size(), (size_t)nk + 1));
+          mips_resize();
           *nc(cur).child_mut(tco) = nk;
           nc(nk) = NodeChildren::Bitmap(UINT64_MAX);
         }
@@ -1266,6 +1298,7 @@ struct Octree {
             }
             uint32_t nk = (uint32_t)push_node(NodeContent{});
             nc_resize(std::max(node_children.size(), nodes.len()));
+            mips_resize();
             *nc(cur).child_mut(tco) = nk;
             node_stack.push_back({nk, tb});
           }
@@ -1293,6 +1326,7 @@ struct Octree {
         set_occupancy_in_bitmap_64bits(to_usize_round(position - nb.min_position), actual_update_size,
                                        as_usize(nb.size), true, &bits);
       store_occupied_bits(node_key, bits);
+      update_mip(node_key, nb, upos);  // insert.rs:370-371
       ContentKind k = nodes.get(node_key).kind;
       if (k == C_LEAF || k == C_UNIFORM) {
         simplifyable = simplify(node_key);
@@ -1416,6 +1450,7 @@ struct Octree {
         nc(node_key) = NodeChildren{};
       else
         store_occupied_bits(node_key, bits);
+      update_mip(node_key, nb, position);  // clear.rs:334-335
       if (simplifyable) simplifyable = simplify(node_key);
       if (previous == bits) break;
     }
@@ -1429,12 +1464,11 @@ struct Octree {
   }
   static uint8_t child_octant_for(const Cube& b, V3f p) { return hash_region(p - b.min_position, b.size / 2.0f); }
 
-  // octree/mod.rs:416-578
-  Entry get(const uint32_t upos[3]) {
+  // octree/mod.rs:416-578 (get = get_internal from the root)
+  Entry get(const uint32_t upos[3]) { return get_internal(0, root_bounds((float)octree_size), upos); }
+  Entry get_internal(size_t cur, Cube cb, const uint32_t upos[3]) {
     V3f position{(float)upos[0], (float)upos[1], (float)upos[2]};
-    Cube cb = root_bounds((float)octree_size);
     if (!bound_contains(cb, position)) return Entry{};
-    size_t cur = 0;
     for (;;) {
       NodeContent& n = nodes.get(cur);
       switch (n.kind) {
@@ -1473,6 +1507,299 @@ struct Octree {
         }
       }
     }
+  }
+
+
+  // ---------------- MIP maps (octree/mipmap.rs) ----------------
+  // MIPResaplingFunction::execute (:131-273) over the sample_size^3 cells from sample_start, x
+  // outermost.  PointFilter and Posterize keep their candidates in a HashMap whose iteration order
+  // Rust randomises per process: the winner among equally frequent colours (and, for Posterize,
+  // which of several matching groups a colour joins) is not defined by the reference; here the
+  // groups are kept in first-seen order and the first group with the highest count wins.
+  template <class F>
+  static bool mip_resample(MipSampler sampler, V3u start, uint32_t size, F sample, uint32_t* out) {
+    switch (sampler.method) {
+      case MIP_BOX: {
+        bool any = false;
+        uint32_t count = 0;
+        float acc[4] = {0, 0, 0, 0};
+        for (uint64_t x = start.x; x < start.x + size; ++x)
+          for (uint64_t y = start.y; y < start.y + size; ++y)
+            for (uint64_t z = start.z; z < start.z + size; ++z) {
+              uint32_t c;
+              if (!sample(V3u{x, y, z}, &c)) continue;
+              const float v[4] = {(float)(c >> 24), (float)((c >> 16) & 0xFF), (float)((c >> 8) & 0xFF), (float)(c & 0xFF)};
+              if (!any) {
+                any = true;
+                count = 1;
+                for (int k = 0; k < 4; ++k) acc[k] = v[k] * v[k];  // powf(2.) is exact as v * v
+              } else {
+                ++count;
+                for (int k = 0; k < 4; ++k) acc[k] += v[k] * v[k];
+              }
+            }
+        if (!any) return false;
+        uint32_t ch[4];
+        for (int k = 0; k < 4; ++k) ch[k] = sat_u8(std::fmin(std::sqrt(acc[k] / (float)count), 255.0f));
+        *out = (ch[0] << 24) | (ch[1] << 16) | (ch[2] << 8) | ch[3];
+        return true;
+      }
+      case MIP_POINT:
+      case MIP_POINT_BD: {
+        std::vector<std::pair<uint32_t, uint32_t>> counts;  // (colour, occurrences), first-seen order
+        for (uint64_t x = start.x; x < start.x + size; ++x)
+          for (uint64_t y = start.y; y < start.y + size; ++y)
+            for (uint64_t z = start.z; z < start.z + size; ++z) {
+              uint32_t c;
+              if (!sample(V3u{x, y, z}, &c)) continue;
+              bool found = false;
+              for (auto& e : counts)
+                if (e.first == c) {
+                  ++e.second;
+                  found = true;
+                  break;
+                }
+              if (!found) counts.push_back({c, 1});
+            }
+        if (counts.empty()) return false;
+        size_t best = 0;
+        for (size_t i = 1; i < counts.size(); ++i)
+          if (counts[i].second > counts[best].second) best = i;
+        *out = counts[best].first;
+        return true;
+      }
+      default: {  // Posterize, PosterizeBD
+        struct Group {
+          uint32_t sum[4];  // squared channel sums (Albedou32)
+          uint32_t count;
+        };
+        std::vector<Group> groups;
+        auto poster = [](const Group& g, uint32_t k) {  // (sum / count).sqrt(), channel k
+          const uint32_t avg = round_u32((float)g.sum[k] / (float)g.count);
+          return round_u32(std::sqrt((float)avg));
+        };
+        for (uint64_t x = start.x; x < start.x + size; ++x)
+          for (uint64_t y = start.y; y < start.y + size; ++y)
+            for (uint64_t z = start.z; z < start.z + size; ++z) {
+              uint32_t c;
+              if (!sample(V3u{x, y, z}, &c)) continue;
+              const uint32_t v[4] = {c >> 24, (c >> 16) & 0xFF, (c >> 8) & 0xFF, c & 0xFF};
+              bool joined = false;
+              for (auto& g : groups) {
+                uint32_t d[4];
+                for (int k = 0; k < 4; ++k) d[k] = poster(g, k) - v[k];  // u32 wrap-around like the reference's Sub
+                const float len = std::sqrt((float)(d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + d[3] * d[3]));
+                if (len < sampler.thr * 255.0f) {
+                  for (int k = 0; k < 4; ++k) g.sum[k] += v[k] * v[k];
+                  ++g.count;
+                  joined = true;
+                  break;
+                }
+              }
+              if (!joined) groups.push_back(Group{{v[0] * v[0], v[1] * v[1], v[2] * v[2], v[3] * v[3]}, 1});
+            }
+        if (groups.empty()) return false;
+        size_t best = 0;
+        for (size_t i = 1; i < groups.size(); ++i)
+          if (groups[i].count > groups[best].count) best = i;
+        uint32_t ch[4];
+        for (int k = 0; k < 4; ++k) ch[k] = std::min<uint32_t>(poster(groups[best], k), 255);
+        *out = (ch[0] << 24) | (ch[1] << 16) | (ch[2] << 8) | ch[3];
+        return true;
+      }
+    }
+  }
+  static uint32_t sat_u8(float v) {  // `f32 as u8`
+    if (!(v > 0.0f)) return 0;
+    if (v >= 255.0f) return 255;
+    return (uint32_t)v;
+  }
+  static uint32_t round_u32(float v) {  // `f32.round() as u32`
+    return as_u32(std::round(v));
+  }
+  // Albedo::distance_from (detail.rs:82-89)
+  static float albedo_distance(uint32_t a, uint32_t b) {
+    const float dr = (float)(a >> 24) - (float)(b >> 24), dg = (float)((a >> 16) & 0xFF) - (float)((b >> 16) & 0xFF);
+    const float db = (float)((a >> 8) & 0xFF) - (float)((b >> 8) & 0xFF), da = (float)(a & 0xFF) - (float)(b & 0xFF);
+    return std::sqrt(((dr * dr + dg * dg) + db * db) + da * da);
+  }
+
+  // Octree::update_mip (mipmap.rs:309-577)
+  void update_mip(size_t node_key, const Cube& node_bounds, const uint32_t upos[3]) {
+    if (!mips_enabled) return;
+    const V3u position{upos[0], upos[1], upos[2]};
+    const size_t mip_level = as_usize(std::log2(node_bounds.size / (float)brick_dim));
+    auto mit = mip_methods.find(mip_level);
+    const bool dominant_bottom = mit != mip_methods.end() && mit->second.method == MIP_POINT_BD;
+    const MipSampler sampler = mit != mip_methods.end() ? mit->second : MipSampler{MIP_BOX, 0.0f};
+    const NodeContent& n = nodes.get(node_key);
+    V3u sample_start{0, 0, 0};
+    uint32_t sample_size = 0;
+    switch (n.kind) {
+      case C_NOTHING: return;
+      case C_UNIFORM:
+        // a UniformLeaf's content is its own MIP
+        if (mip(node_key).kind != B_EMPTY) mip(node_key) = BrickData::Empty();
+        return;
+      case C_LEAF: {
+        sample_size = std::min<uint32_t>(as_u32(node_bounds.size) / brick_dim, brick_dim * 2);
+        const float f = node_bounds.size;
+        const uint64_t px = (position.x - position.x % sample_size) * 2 * brick_dim;
+        const uint64_t py = (position.y - position.y % sample_size) * 2 * brick_dim;
+        const uint64_t pz = (position.z - position.z % sample_size) * 2 * brick_dim;
+        sample_start = V3u{round_u32(std::floor((float)(uint32_t)px / f)), round_u32(std::floor((float)(uint32_t)py / f)),
+                           round_u32(std::floor((float)(uint32_t)pz / f))};
+        break;
+      }
+      default:
+        if (dominant_bottom) {
+          sample_size = as_u32(node_bounds.size) / brick_dim;
+          sample_start = V3u{position.x - position.x % sample_size, position.y - position.y % sample_size,
+                             position.z - position.z % sample_size};
+        } else {
+          sample_size = 2;
+          const V3f pib{(float)position.x - node_bounds.min_position.x, (float)position.y - node_bounds.min_position.y,
+                        (float)position.z - node_bounds.min_position.z};
+          const float D = (float)brick_dim;
+          V3u ss{round_u32(std::floor(pib.x * 2.0f * D / node_bounds.size)),
+                 round_u32(std::floor(pib.y * 2.0f * D / node_bounds.size)),
+                 round_u32(std::floor(pib.z * 2.0f * D / node_bounds.size))};
+          sample_start = V3u{ss.x - ss.x % 2, ss.y - ss.y % 2, ss.z - ss.z % 2};
+        }
+    }
+    uint32_t color = 0;
+    bool sampled = false;
+    if (n.kind == C_LEAF || dominant_bottom) {
+      sampled = mip_resample(sampler, sample_start, sample_size, [&](V3u p, uint32_t* c) {
+        const uint32_t up[3] = {(uint32_t)p.x, (uint32_t)p.y, (uint32_t)p.z};
+        const Entry e = get_internal(node_key, node_bounds, up);
+        if (!(e.kind & 1u)) return false;
+        *c = e.rgba;
+        return true;
+      }, &color);
+    } else {
+      // the sampling range spans 0 .. 2 * brick_dim over the children's MIPs
+      const float D = (float)brick_dim;
+      const uint8_t first = hash_region(V3f{(float)sample_start.x, (float)sample_start.y, (float)sample_start.z}, D);
+      if (nc(node_key).child(first) != EMPTY_U32) {
+        sampled = mip_resample(sampler, sample_start, sample_size, [&](V3u p, uint32_t* c) {
+          const uint8_t o = hash_region(V3f{(float)p.x, (float)p.y, (float)p.z}, D);
+          const uint64_t ck = nc(node_key).child(o);
+          if (ck == EMPTY_U32) return false;
+          const V3f off = OCTANT_OFFSET_REGION_LUT[o] * D;
+          const V3u q{p.x - round_u32(off.x), p.y - round_u32(off.y), p.z - round_u32(off.z)};
+          const BrickData& m = mip(ck);
+          Entry e;
+          if (m.kind == B_EMPTY) return false;
+          if (m.kind == B_SOLID) {
+            e = pix_get_ref(m.solid);
+          } else {
+            const size_t fi = flat_projection(q.x, q.y, q.z, brick_dim);
+            if (fi >= m.parted.size()) throw Panic("MIP brick index out of bounds");
+            e = pix_get_ref(m.parted[fi]);
+          }
+          if (!(e.kind & 1u)) return false;
+          *c = e.rgba;
+          return true;
+        }, &color);
+      }
+    }
+    if (!sampled) return;
+    // assemble the MIP entry (:519-545)
+    uint32_t entry;
+    auto thr = mip_color_thr.find(mip_level);
+    if (thr != mip_color_thr.end()) {
+      const float limit = thr->second * 255.0f;
+      size_t similar = SIZE_MAX;
+      for (size_t i = 0; i < color_palette.size(); ++i)
+        if (albedo_distance(color, color_palette[i]) < limit) {
+          similar = i;
+          break;
+        }
+      entry = similar != SIZE_MAX ? pix_visual((uint32_t)(uint16_t)similar) : add_to_palette(Entry{1, color, 0});
+    } else {
+      entry = add_to_palette(Entry{1, color, 0});
+    }
+    const V3u pim = matrix_index_for(node_bounds, upos, brick_dim);
+    const size_t fi = flat_projection(pim.x, pim.y, pim.z, brick_dim);
+    const size_t len = (size_t)brick_dim * brick_dim * brick_dim;
+    BrickData& m = mip(node_key);
+    if (m.kind == B_EMPTY) {
+      std::vector<uint32_t> b(len, EMPTY_U32);
+      b[fi] = entry;
+      m = BrickData::Parted(std::move(b));
+    } else if (m.kind == B_SOLID) {
+      std::vector<uint32_t> b(len, m.solid);
+      b[fi] = entry;
+      m = BrickData::Parted(std::move(b));
+    } else {
+      if (fi >= m.parted.size()) throw Panic("MIP brick index out of bounds");
+      m.parted[fi] = entry;
+    }
+  }
+
+  // StrategyUpdater::recalculate_mip (mipmap.rs:882-899)
+  void recalculate_mip(size_t node_key, const Cube& b) {
+    if (!mips_enabled) return;
+    const float D = (float)brick_dim;
+    for (uint32_t x = 0; x < brick_dim; ++x)
+      for (uint32_t y = 0; y < brick_dim; ++y)
+        for (uint32_t z = 0; z < brick_dim; ++z) {
+          const V3f off{std::round((float)x * b.size / D), std::round((float)y * b.size / D),
+                        std::round((float)z * b.size / D)};
+          const V3f pos = b.min_position + off;
+          const uint32_t up[3] = {round_u32(pos.x), round_u32(pos.y), round_u32(pos.z)};
+          update_mip(node_key, b, up);
+        }
+  }
+  // StrategyUpdater::recalculate_mips (mipmap.rs:798-856)
+  void recalculate_mips() {
+    node_mips.assign(nodes.len(), BrickData{});
+    struct SE {
+      size_t key;
+      Cube b;
+      uint32_t octant;
+    };
+    std::vector<SE> st{{0, root_bounds((float)octree_size), 0}};
+    while (!st.empty()) {
+      SE& top = st.back();
+      if (top.octant == OOB_OCTANT) {
+        recalculate_mip(top.key, top.b);
+        st.pop_back();
+        if (!st.empty()) st.back().octant += 1;
+        continue;
+      }
+      const NodeContent& n = nodes.get(top.key);
+      if (n.kind == C_NOTHING) throw Panic("BFS shouldn't evaluate empty children");
+      if (n.kind == C_INTERNAL) {
+        const uint64_t ck = nc(top.key).child((uint8_t)top.octant);
+        if (nodes.key_is_valid(ck) && nodes.get(ck).kind != C_NOTHING) {
+          const SE child{(size_t)ck, child_bounds_for(top.b, (uint8_t)top.octant), 0};
+          st.push_back(child);
+        } else {
+          top.octant += 1;
+        }
+      } else {
+        top.octant = OOB_OCTANT;
+      }
+    }
+  }
+  // StrategyUpdater::switch_albedo_mip_maps (mipmap.rs:858-880)
+  void switch_albedo_mip_maps(bool enabled) {
+    const bool before = mips_enabled;
+    mips_enabled = enabled;
+    if (mips_enabled && before != enabled && nodes.get(0).kind != C_NOTHING) recalculate_mips();
+  }
+  // StrategyUpdater::sample_root_mip (mipmap.rs:905-937)
+  Entry sample_root_mip(uint8_t octant, const uint32_t p[3]) {
+    const uint64_t key = octant == OOB_OCTANT ? 0 : nc(0).child(octant);
+    if (!nodes.key_is_valid(key)) return Entry{};
+    const BrickData& m = mip(key);
+    if (m.kind == B_EMPTY) return Entry{};
+    if (m.kind == B_SOLID) return pix_get_ref(m.solid);
+    const size_t fi = flat_projection(p[0], p[1], p[2], brick_dim);
+    if (fi >= m.parted.size()) throw Panic("MIP brick index out of bounds");
+    return pix_get_ref(m.parted[fi]);
   }
 
   // ---------------- the cast (raytracing/raytracing_on_cpu.rs) ----------------
@@ -1586,11 +1913,12 @@ struct Octree {
   };
 
   // :316-565 (get_by_ray -> get_by_ray_at_lod with MIPs disabled)
-  CastResult get_by_ray(const Ray& ray) const {
+  // get_by_ray is get_by_ray_at_lod(ray, f32::MAX) (:316-318)
+  CastResult get_by_ray(const Ray& ray, float viewing_distance = FLT_MAX) const {
     CastResult res;
     uint64_t work = 0;
     try {
-      if (cast_inner(ray, res, work))
+      if (cast_inner(ray, viewing_distance, res, work))
         res.status = 1;
       else
         res.status = 0;
@@ -1604,7 +1932,7 @@ struct Octree {
     return res;
   }
 
-  bool cast_inner(const Ray& ray, CastResult& res, uint64_t& work) const {
+  bool cast_inner(const Ray& ray, float viewing_distance, CastResult& res, uint64_t& work) const {
     const Luts& L = luts();
     const V3f sf = get_dda_scale_factors(ray);
     const uint8_t dir_idx = hash_direction(ray.direction);
@@ -1632,6 +1960,7 @@ struct Octree {
       if (ix >= 4 || iy >= 4 || iz >= 4) throw Panic("BITMAP_INDEX_LUT index out of bounds");
       return L.bitmap_index[ix][iy][iz];
     };
+    float mip_level = std::log2((float)octree_size / (float)brick_dim);  // :350, kept across restarts
     while (target_octant != OOB_OCTANT) {
       cur = 0;
       cb = root_bounds(S);
@@ -1656,6 +1985,18 @@ struct Octree {
         }
         const NodeContent& cn = node(cur);
         bool backtrack = cn.kind == C_UNIFORM;
+        // the node's MIP when its level is below the one the travelled distance asks for (:366-386)
+        if (mips_enabled) {
+          const float m2 = mip_level * 2.0f;
+          const V3f al{std::round(p.x / m2) * m2, std::round(p.y / m2) * m2, std::round(p.z / m2) * m2};
+          if (mip_level < length(ray.origin - al) / viewing_distance) {
+            if (probe_brick(ray, p, mip(cur), cb, sf, res, work)) {
+              res.node_key = (uint32_t)cur;
+              res.brick_octant = 8;  // the node's MIP brick
+              return true;
+            }
+          }
+        }
         if (target_octant != OOB_OCTANT) {
           if (cn.kind == C_UNIFORM) {
             if (probe_brick(ray, p, cn.bricks[0], cb, sf, res, work)) {
@@ -1680,6 +2021,7 @@ struct Octree {
         if (backtrack || target_octant == OOB_OCTANT || occ == 0 || (occ & L.ray_to_node[flat_pos][dir_idx]) == 0) {
           // POP (:445-473)
           stack.pop();
+          mip_level += 1.0f;
           uint32_t parent;
           if (stack.last(&parent)) {
             cur = parent;
@@ -1703,6 +2045,7 @@ struct Octree {
           cb = tb;
           target_octant = hash_region(p - tb.min_position, tb.size / 2.0f);
           stack.push((uint32_t)tck);
+          mip_level -= 1.0f;
         } else {
           // ADVANCE (:494-544)
           for (;;) {
@@ -1828,12 +2171,17 @@ int orc_get(void* tree, uint32_t x, uint32_t y, uint32_t z, uint32_t out[3]) {
 
 int orc_cast(void* tree, uint64_t n, const float* ox, const float* oy, const float* oz, const float* dx,
              const float* dy, const float* dz, const orc_hits* out, int threads) {
+  return orc_cast_lod(tree, n, ox, oy, oz, dx, dy, dz, FLT_MAX, out, threads);
+}
+
+int orc_cast_lod(void* tree, uint64_t n, const float* ox, const float* oy, const float* oz, const float* dx,
+                 const float* dy, const float* dz, float viewing_distance, const orc_hits* out, int threads) {
   const Octree* t = static_cast<const Octree*>(tree);
   if (!t || !out) return ORC_ERR_ARGUMENT;
   auto work = [&](uint64_t b, uint64_t e) {
     for (uint64_t i = b; i < e; ++i) {
       Ray r{V3f{ox[i], oy[i], oz[i]}, V3f{dx[i], dy[i], dz[i]}};
-      Octree::CastResult h = t->get_by_ray(r);
+      Octree::CastResult h = t->get_by_ray(r, viewing_distance);
       if (out->status) out->status[i] = h.status;
       if (out->brick_octant) out->brick_octant[i] = h.brick_octant;
       if (out->entry_kind) out->entry_kind[i] = (uint8_t)h.entry.kind;
@@ -1936,6 +2284,55 @@ int orc_render_viewport(void* tree, const orc_viewport* vp, uint32_t W, uint32_t
 }
 
 uint64_t orc_node_count(void* tree) { return static_cast<Octree*>(tree)->nodes.len(); }
+
+// ---- MIP maps (octree/mipmap.rs, the StrategyUpdater of octree/mod.rs) ----
+int orc_mip_switch(void* tree, int enabled) {
+  return guarded([&] {
+    static_cast<Octree*>(tree)->switch_albedo_mip_maps(enabled != 0);
+    return ORC_OK;
+  });
+}
+int orc_mip_set_method(void* tree, uint32_t level, uint32_t method, float thr) {
+  if (method > 4) return ORC_ERR_ARGUMENT;
+  Octree* t = static_cast<Octree*>(tree);
+  if (method >= 3) thr = std::min(std::max(thr, 0.0f), 1.0f);  // set_method_at_internal clamps thresholds
+  t->mip_methods[level] = Octree::MipSampler{(Octree::MipMethod)method, thr};
+  return ORC_OK;
+}
+int orc_mip_set_color_threshold(void* tree, uint32_t level, float thr) {
+  static_cast<Octree*>(tree)->mip_color_thr[level] = std::min(std::max(thr, 0.0f), 1.0f);
+  return ORC_OK;
+}
+int orc_mip_recalculate(void* tree) {
+  return guarded([&] {
+    static_cast<Octree*>(tree)->recalculate_mips();
+    return ORC_OK;
+  });
+}
+int orc_mip_sample_root(void* tree, uint32_t octant, uint32_t x, uint32_t y, uint32_t z, uint32_t out[3]) {
+  const uint32_t p[3] = {x, y, z};
+  return guarded([&] {
+    Entry e = static_cast<Octree*>(tree)->sample_root_mip((uint8_t)octant, p);
+    out[0] = e.kind;
+    out[1] = e.rgba;
+    out[2] = e.user;
+    return ORC_OK;
+  });
+}
+// The MIP brick of a node: kind (0 empty, 1 solid, 2 parted, 3 no entry: past node_mips), its
+// solid value or brick_dim^3 values into `values` (when not NULL).
+int orc_node_mip(void* tree, uint64_t key, uint32_t* kind, uint32_t* values) {
+  const Octree* t = static_cast<const Octree*>(tree);
+  if (key >= t->node_mips.size()) {
+    *kind = 3;
+    return ORC_OK;
+  }
+  const BrickData& m = t->node_mips[key];
+  *kind = m.kind == B_EMPTY ? 0u : (m.kind == B_SOLID ? 1u : 2u);
+  if (values && m.kind == B_SOLID) values[0] = m.solid;
+  if (values && m.kind == B_PARTED) std::copy(m.parted.begin(), m.parted.end(), values);
+  return ORC_OK;
+}
 
 static uint64_t fnv_brick(const std::vector<uint32_t>& v) {
   uint64_t h = 1469598103934665603ull;

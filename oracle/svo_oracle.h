@@ -94,6 +94,19 @@ typedef struct {
 int orc_render_viewport(void* tree, const orc_viewport* vp, uint32_t width_px, uint32_t height_px, uint8_t* rgba,
                         uint64_t* unshaded, int threads);
 
+/* get_by_ray_at_lod (raytracing_on_cpu.rs:325-565): the cast with a viewing distance; orc_cast is
+   this with f32::MAX.  A hit on a node's MIP brick reports brick_octant 8. */
+int orc_cast_lod(void* tree, uint64_t n, const float* ox, const float* oy, const float* oz, const float* dx,
+                 const float* dy, const float* dz, float viewing_distance, const orc_hits* out, int threads);
+/* MIP maps (octree/mipmap.rs).  method: 0 BoxFilter, 1 PointFilter, 2 PointFilterBD, 3 Posterize(thr),
+   4 PosterizeBD(thr). */
+int orc_mip_switch(void* tree, int enabled);
+int orc_mip_set_method(void* tree, uint32_t level, uint32_t method, float thr);
+int orc_mip_set_color_threshold(void* tree, uint32_t level, float thr);
+int orc_mip_recalculate(void* tree);
+int orc_mip_sample_root(void* tree, uint32_t octant, uint32_t x, uint32_t y, uint32_t z, uint32_t out_kind_rgba_user[3]);
+int orc_node_mip(void* tree, uint64_t key, uint32_t* kind, uint32_t* values);
+
 uint64_t orc_node_count(void* tree);
 int orc_node_record(void* tree, uint64_t key, uint64_t rec[40]);
 uint64_t orc_palette(void* tree, int which, uint32_t* out, uint64_t max);
