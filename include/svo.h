@@ -129,6 +129,28 @@ svo_status svo_apply_ops(svo_scene* scene, const svo_op* ops, uint64_t n, uint64
 /* Octree::get (src/octree/mod.rs:416-422) */
 svo_status svo_get(svo_scene* scene, uint32_t x, uint32_t y, uint32_t z, uint32_t* kind, uint32_t* rgba, uint32_t* user);
 svo_status svo_scene_stats_get(svo_scene* scene, svo_scene_stats* out);
+
+/* ---- MIP maps: the StrategyUpdater of Octree::albedo_mip_map_resampling_strategy()
+ *      (src/octree/mipmap.rs:609-880; disabled by default) ---------------------------- */
+typedef enum {
+  SVO_MIP_BOX_FILTER = 0,     /* MIPResamplingMethods::BoxFilter */
+  SVO_MIP_POINT_FILTER = 1,   /* PointFilter */
+  SVO_MIP_POINT_FILTER_BD = 2, /* PointFilterBD */
+  SVO_MIP_POSTERIZE = 3,      /* Posterize(threshold) */
+  SVO_MIP_POSTERIZE_BD = 4    /* PosterizeBD(threshold) */
+} svo_mip_method;
+/* switch_albedo_mip_maps: enabling recalculates every MIP (when the root is not empty); while
+ * enabled, insert and clear update the MIPs on their path. */
+svo_status svo_mip_switch(svo_scene* scene, int32_t enabled);
+/* set_method_at: the resampling method of one MIP level (threshold clamped to 0..1). */
+svo_status svo_mip_set_method(svo_scene* scene, uint32_t level, uint32_t method, float threshold);
+/* set_color_similarity_thr_at: colours closer than threshold * 255 reuse a palette entry. */
+svo_status svo_mip_set_color_threshold(svo_scene* scene, uint32_t level, float threshold);
+/* recalculate_mips */
+svo_status svo_mip_recalculate(svo_scene* scene);
+/* sample_root_mip: the root's MIP (octant 8) or a root child's, at a position inside the MIP. */
+svo_status svo_mip_sample_root(svo_scene* scene, uint32_t octant, uint32_t x, uint32_t y, uint32_t z, uint32_t* kind,
+                               uint32_t* rgba, uint32_t* user);
 /* Canonical per-node record used to compare structures (key, content, children, bricks). */
 svo_status svo_node_record(svo_scene* scene, uint64_t key, uint64_t rec[40]);
 /* Copies palette `which` (0 colours, 1 user data); returns its length. */

@@ -2367,6 +2367,14 @@ int orc_node_record(void* tree, uint64_t key, uint64_t rec[40]) {
     rec[21 + i] = b.kind == B_SOLID ? b.solid : 0;
     rec[29 + i] = b.kind == B_PARTED ? fnv_brick(b.parted) : 0;
   }
+  if (key >= t->node_mips.size()) {
+    rec[37] = 3;
+  } else {
+    const BrickData& m = t->node_mips[key];
+    rec[37] = m.kind;
+    rec[38] = m.kind == B_SOLID ? m.solid : 0;
+    rec[39] = m.kind == B_PARTED ? fnv_brick(m.parted) : 0;
+  }
   return ORC_OK;
 }
 

@@ -158,6 +158,32 @@ class Octree:
         h = Hits(**{k: _vp(out[k].ctypes.data) if k in out else None for k in HIT_FIELDS})
         check(lib().svo_cast_host(self._h, ctypes.byref(r), n, ctypes.byref(h), _vp(stream)))
 
+    # ---- MIP maps: Octree::albedo_mip_map_resampling_strategy() (src/octree/mipmap.rs) ----
+    BOX_FILTER, POINT_FILTER, POINT_FILTER_BD, POSTERIZE, POSTERIZE_BD = range(5)
+
+    def switch_albedo_mip_maps(self, enabled):
+        check(lib().svo_mip_switch(self._h, int(bool(enabled))))
+        return self
+
+    def set_mip_method(self, level, method, threshold=0.0):
+        check(lib().svo_mip_set_method(self._h, level, method, threshold))
+        return self
+
+    def set_mip_color_threshold(self, level, threshold):
+        check(lib().svo_mip_set_color_threshold(self._h, level, threshold))
+        return self
+
+    def recalculate_mips(self):
+        check(lib().svo_mip_recalculate(self._h))
+        return self
+
+    def sample_root_mip(self, octant, pos):
+        """(kind, rgba, user) of the root's MIP (octant 8) or a root child's at `pos`."""
+        k, a, u = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        check(lib().svo_mip_sample_root(self._h, octant, pos[0], pos[1], pos[2], ctypes.byref(k), ctypes.byref(a),
+                                        ctypes.byref(u)))
+        return k.value, a.value, u.value
+
     def render_viewport(self, viewport, width, height, rgba, unshaded=0, stream=0):
         """Fused render of examples/cpu_render.rs's frame into device memory: `viewport` from
         viewport(), `rgba` a device pointer to height * width * 4 bytes (row-major from the top

@@ -100,6 +100,11 @@ SIGNATURES = {
     "svo_get": (_I32, [_VP, _U32, _U32, _U32, _P(_U32), _P(_U32), _P(_U32)]),
     "svo_scene_stats_get": (_I32, [_VP, _P(SceneStats)]),
     "svo_node_record": (_I32, [_VP, _U64, _P(_U64)]),
+    "svo_mip_switch": (_I32, [_VP, _I32]),
+    "svo_mip_set_method": (_I32, [_VP, _U32, _U32, ctypes.c_float]),
+    "svo_mip_set_color_threshold": (_I32, [_VP, _U32, ctypes.c_float]),
+    "svo_mip_recalculate": (_I32, [_VP]),
+    "svo_mip_sample_root": (_I32, [_VP, _U32, _U32, _U32, _U32, _P(_U32), _P(_U32), _P(_U32)]),
     "svo_palette": (_U64, [_VP, _I32, _VP, _U64]),
     "svo_scene_upload": (_I32, [_VP, _VP]),
     "svo_scene_sync": (_I32, [_VP, _VP]),

@@ -72,6 +72,50 @@ svo_status svo_set_auto_simplify(svo_scene* s, int32_t enabled) {
   return SVO_OK;
 }
 
+// ---- MIP maps: Octree::albedo_mip_map_resampling_strategy() (src/octree/mipmap.rs) ----
+svo_status svo_mip_switch(svo_scene* s, int32_t enabled) {
+  if (!s) return fail(SVO_ERR_ARGUMENT, "NULL scene");
+  return guarded("svo_mip_switch", [&] {
+    s->tree.switch_albedo_mip_maps(enabled != 0);
+    return SVO_OK;
+  });
+}
+
+svo_status svo_mip_set_method(svo_scene* s, uint32_t level, uint32_t method, float threshold) {
+  if (!s) return fail(SVO_ERR_ARGUMENT, "NULL scene");
+  if (method > SVO_MIP_POSTERIZE_BD) return fail(SVO_ERR_ARGUMENT, "svo_mip_set_method: unknown method");
+  s->tree.set_mip_method(level, method, threshold);
+  return SVO_OK;
+}
+
+svo_status svo_mip_set_color_threshold(svo_scene* s, uint32_t level, float threshold) {
+  if (!s) return fail(SVO_ERR_ARGUMENT, "NULL scene");
+  s->tree.set_mip_color_threshold(level, threshold);
+  return SVO_OK;
+}
+
+svo_status svo_mip_recalculate(svo_scene* s) {
+  if (!s) return fail(SVO_ERR_ARGUMENT, "NULL scene");
+  return guarded("svo_mip_recalculate", [&] {
+    s->tree.recalculate_mips();
+    return SVO_OK;
+  });
+}
+
+svo_status svo_mip_sample_root(svo_scene* s, uint32_t octant, uint32_t x, uint32_t y, uint32_t z, uint32_t* kind,
+                               uint32_t* rgba, uint32_t* user) {
+  if (!s || !kind || !rgba || !user) return fail(SVO_ERR_ARGUMENT, "NULL argument");
+  if (octant > 8) return fail(SVO_ERR_ARGUMENT, "svo_mip_sample_root: octant must be 0..8");
+  const uint32_t p[3] = {x, y, z};
+  return guarded("svo_mip_sample_root", [&] {
+    const Entry e = s->tree.sample_root_mip((uint8_t)octant, p);
+    *kind = e.kind;
+    *rgba = e.rgba;
+    *user = e.user;
+    return SVO_OK;
+  });
+}
+
 svo_status svo_insert(svo_scene* s, uint32_t x, uint32_t y, uint32_t z, uint32_t kind, uint32_t rgba, uint32_t user) {
   if (!s) return fail(SVO_ERR_ARGUMENT, "NULL scene");
   const uint32_t p[3] = {x, y, z};

@@ -143,6 +143,10 @@ int HostOctree::create(uint32_t size, uint32_t dim, HostOctree* t) {
   t->dim = dim;
   t->arena.init(dim);
   t->push(Content{});  // root key 0 (mod.rs:397)
+  t->mips.assign(1, BrickRef{});  // node_mips: vec![BrickData::Empty] (mod.rs:198)
+  // MIPMapStrategy::default (mipmap.rs:580-595)
+  t->mip_methods = {{1, {kMipPoint, 0.0f}}, {2, {kMipBox, 0.0f}}, {3, {kMipBox, 0.0f}}, {4, {kMipBox, 0.0f}}};
+  t->mip_color_thr = {{2, 0.1f}, {3, 0.05f}, {4, 0.02f}};
   return 0;
 }
 
@@ -627,12 +631,16 @@ void HostOctree::subdivide_leaf_to_nodes(size_t k, size_t target_octant) {
       BrickRef b = old.b[o];
       old.b[o] = BrickRef{};
       if (b.kind == kBrickEmpty) {
-        if (o == target_octant) nn[o] = (uint32_t)push(Content{});
+        if (o == target_octant) {
+          nn[o] = (uint32_t)push(Content{});
+          mips_resize();
+        }
       } else if (b.kind == kBrickSolid) {
         Content u;
         u.kind = kUniform;
         u.b[0] = b;
         nn[o] = (uint32_t)push(std::move(u));
+        mips_resize();
         set_children_bitmap(nn[o], UINT64_MAX);
       } else {
         // detail.rs:387-394 computes the bitmap from bricks[octant], already swapped out to Empty
@@ -640,6 +648,7 @@ void HostOctree::subdivide_leaf_to_nodes(size_t k, size_t target_octant) {
         u.kind = kUniform;
         u.b[0] = b;
         nn[o] = (uint32_t)push(std::move(u));
+        mips_resize();
         set_children_bitmap(nn[o], 0);
       }
     }
@@ -648,13 +657,14 @@ void HostOctree::subdivide_leaf_to_nodes(size_t k, size_t target_octant) {
     old.b[0] = BrickRef{};
     if (b.kind == kBrickEmpty) {
       nn[target_octant] = (uint32_t)push(Content{});
+      mips_resize();
       set_children_bitmap(nn[target_octant], 0);
     } else if (b.kind == kBrickSolid) {
       for (size_t o = 0; o < 8; ++o) {
         Content u;
         u.kind = kUniform;
         u.b[0] = BrickRef{kBrickSolid, b.v};
-        nn[o] = (uint32_t)push(std::move(u));
+        nn[o] = (uint32_t)push(std::move(u));  // node_mips is not resized here (detail.rs:432-447)
         set_children_bitmap(nn[o], UINT64_MAX);
       }
     } else {
@@ -667,6 +677,7 @@ void HostOctree::subdivide_leaf_to_nodes(size_t k, size_t target_octant) {
         u.kind = kUniform;
         u.b[0] = BrickRef{kBrickParted, slots[o]};
         nn[o] = (uint32_t)push(std::move(u));
+        mips_resize();
         set_children_bitmap(nn[o], bits);
       }
     }
@@ -1001,6 +1012,7 @@ int HostOctree::insert_at_lod(bool overwrite, const uint32_t up[3], uint32_t isz
         set_children_bitmap(tck, UINT64_MAX);
       } else {
         const uint32_t nk = (uint32_t)push(std::move(u));
+        mips_resize();
         *child_mut(cur, to) = nk;
         set_children_bitmap(nk, UINT64_MAX);
       }
@@ -1033,6 +1045,7 @@ int HostOctree::insert_at_lod(bool overwrite, const uint32_t up[3], uint32_t isz
           touch(cur);
         }
         const uint32_t nk = (uint32_t)push(Content{});
+        mips_resize();
         *child_mut(cur, to) = nk;
         stack.push_back({nk, tb});
       }
@@ -1060,6 +1073,7 @@ int HostOctree::insert_at_lod(bool overwrite, const uint32_t up[3], uint32_t isz
       set_occupancy(rel, actual, sat_usize(nb.size), true, &bits);
     }
     store_occupied_bits(k, bits);
+    update_mip(k, nb, up);  // insert.rs:370-371
     if (kind[k] == kLeaf || kind[k] == kUniform) {
       simplifyable = simplify(k);
       continue;
@@ -1187,6 +1201,7 @@ int HostOctree::clear_at_lod(const uint32_t up[3], uint32_t csz) {
       set_children_none(k);
     else
       store_occupied_bits(k, bits);
+    update_mip(k, nb, up);  // clear.rs:334-335
     if (simplifyable) simplifyable = simplify(k);
     if (previous == bits) break;
   }
@@ -1194,11 +1209,12 @@ int HostOctree::clear_at_lod(const uint32_t up[3], uint32_t csz) {
 }
 
 // ---------------------------------------------------------------- get (src/octree/mod.rs:416-578)
-Entry HostOctree::get(const uint32_t up[3]) {
+Entry HostOctree::get(const uint32_t up[3]) { return get_internal(0, Cube{0.0f, 0.0f, 0.0f, (float)size}, up); }
+
+// get_internal (mod.rs:219-300): the entry at a position within node k's bounds
+Entry HostOctree::get_internal(size_t cur, Cube cb, const uint32_t up[3]) {
   const float px = (float)up[0], py = (float)up[1], pz = (float)up[2];
-  Cube cb{0.0f, 0.0f, 0.0f, (float)size};
   if (!contains(cb, px, py, pz)) return Entry{};
-  size_t cur = 0;
   for (;;) {
     check_key(cur);
     switch (kind[cur]) {
@@ -1242,6 +1258,318 @@ Entry HostOctree::get(const uint32_t up[3]) {
   }
 }
 
+
+// ---------------------------------------------------------------- MIP maps (src/octree/mipmap.rs)
+namespace {
+
+uint32_t sat_u8(float v) {  // `f32 as u8`
+  if (!(v > 0.0f)) return 0;
+  if (v >= 255.0f) return 255;
+  return (uint32_t)v;
+}
+uint32_t round_u32(float v) { return sat_u32(std::round(v)); }  // `f32.round() as u32`
+
+// Albedo::distance_from (detail.rs:82-89)
+float albedo_distance(uint32_t a, uint32_t b) {
+  const float dr = (float)(a >> 24) - (float)(b >> 24), dg = (float)((a >> 16) & 0xFFu) - (float)((b >> 16) & 0xFFu);
+  const float db = (float)((a >> 8) & 0xFFu) - (float)((b >> 8) & 0xFFu), da = (float)(a & 0xFFu) - (float)(b & 0xFFu);
+  return std::sqrt(((dr * dr + dg * dg) + db * db) + da * da);
+}
+
+// MIPResaplingFunction::execute (mipmap.rs:131-273) over size^3 cells from start, x outermost.  The
+// reference keeps PointFilter and Posterize candidates in a HashMap whose iteration order Rust
+// randomises per process, so the winner among equally frequent colours (and, for Posterize, which
+// of several matching groups a colour joins) is not defined by it; candidates are kept here in
+// first-seen order and the first one with the highest count wins.
+template <class F>
+bool mip_resample(HostOctree::MipSampler sampler, const uint32_t start[3], uint32_t size, F&& sample, uint32_t* out) {
+  const uint32_t method = sampler.method;
+  if (method == HostOctree::kMipBox) {
+    bool any = false;
+    uint32_t count = 0;
+    float acc[4] = {0, 0, 0, 0};
+    for (uint32_t x = start[0]; x < start[0] + size; ++x)
+      for (uint32_t y = start[1]; y < start[1] + size; ++y)
+        for (uint32_t z = start[2]; z < start[2] + size; ++z) {
+          uint32_t c;
+          if (!sample(x, y, z, &c)) continue;
+          const float v[4] = {(float)(c >> 24), (float)((c >> 16) & 0xFFu), (float)((c >> 8) & 0xFFu), (float)(c & 0xFFu)};
+          ++count;
+          for (int k = 0; k < 4; ++k) acc[k] = any ? acc[k] + v[k] * v[k] : v[k] * v[k];  // powf(2.) == v * v
+          any = true;
+        }
+    if (!any) return false;
+    uint32_t ch[4];
+    for (int k = 0; k < 4; ++k) ch[k] = sat_u8(std::fmin(std::sqrt(acc[k] / (float)count), 255.0f));
+    *out = (ch[0] << 24) | (ch[1] << 16) | (ch[2] << 8) | ch[3];
+    return true;
+  }
+  if (method == HostOctree::kMipPoint || method == HostOctree::kMipPointBD) {
+    std::vector<std::pair<uint32_t, uint32_t>> counts;
+    for (uint32_t x = start[0]; x < start[0] + size; ++x)
+      for (uint32_t y = start[1]; y < start[1] + size; ++y)
+        for (uint32_t z = start[2]; z < start[2] + size; ++z) {
+          uint32_t c;
+          if (!sample(x, y, z, &c)) continue;
+          auto it = std::find_if(counts.begin(), counts.end(), [&](const std::pair<uint32_t, uint32_t>& e) { return e.first == c; });
+          if (it == counts.end())
+            counts.push_back({c, 1});
+          else
+            ++it->second;
+        }
+    if (counts.empty()) return false;
+    size_t best = 0;
+    for (size_t i = 1; i < counts.size(); ++i)
+      if (counts[i].second > counts[best].second) best = i;
+    *out = counts[best].first;
+    return true;
+  }
+  // Posterize / PosterizeBD: groups of squared channel sums (Albedou32, u32 arithmetic wrapping
+  // like the release build)
+  struct Group {
+    uint32_t sum[4];
+    uint32_t count;
+  };
+  auto poster = [](const Group& g, int k) { return round_u32(std::sqrt((float)round_u32((float)g.sum[k] / (float)g.count))); };
+  std::vector<Group> groups;
+  for (uint32_t x = start[0]; x < start[0] + size; ++x)
+    for (uint32_t y = start[1]; y < start[1] + size; ++y)
+      for (uint32_t z = start[2]; z < start[2] + size; ++z) {
+        uint32_t c;
+        if (!sample(x, y, z, &c)) continue;
+        const uint32_t v[4] = {c >> 24, (c >> 16) & 0xFFu, (c >> 8) & 0xFFu, c & 0xFFu};
+        bool joined = false;
+        for (Group& g : groups) {
+          uint32_t d[4];
+          for (int k = 0; k < 4; ++k) d[k] = poster(g, k) - v[k];
+          if (std::sqrt((float)(d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + d[3] * d[3])) < sampler.thr * 255.0f) {
+            for (int k = 0; k < 4; ++k) g.sum[k] += v[k] * v[k];
+            ++g.count;
+            joined = true;
+            break;
+          }
+        }
+        if (!joined) groups.push_back(Group{{v[0] * v[0], v[1] * v[1], v[2] * v[2], v[3] * v[3]}, 1});
+      }
+  if (groups.empty()) return false;
+  size_t best = 0;
+  for (size_t i = 1; i < groups.size(); ++i)
+    if (groups[i].count > groups[best].count) best = i;
+  uint32_t ch[4];
+  for (int k = 0; k < 4; ++k) ch[k] = std::min<uint32_t>(poster(groups[best], k), 255);
+  *out = (ch[0] << 24) | (ch[1] << 16) | (ch[2] << 8) | ch[3];
+  return true;
+}
+
+}  // namespace
+
+void HostOctree::set_mip(size_t k, BrickRef b) {
+  BrickRef& m = mip(k);
+  if (m.kind == kBrickParted && !(b.kind == kBrickParted && b.v == m.v)) arena.release(m.v);
+  m = b;
+  touch(k);
+}
+
+// Octree::update_mip (mipmap.rs:309-577)
+void HostOctree::update_mip(size_t k, const Cube& nb, const uint32_t up[3]) {
+  if (!mips_enabled) return;
+  const size_t level = sat_usize(std::log2(nb.size / (float)dim));
+  const MipSampler* found = nullptr;
+  for (const auto& e : mip_methods)
+    if (e.first == level) found = &e.second;
+  const bool dominant_bottom = found && found->method == kMipPointBD;
+  const MipSampler sampler = found ? *found : MipSampler{kMipBox, 0.0f};
+  check_key(k);
+  uint32_t start[3] = {0, 0, 0}, ssize = 0;
+  switch (kind[k]) {
+    case kNothing: return;
+    case kUniform:  // a UniformLeaf's content is its own MIP
+      if (mip(k).kind != kBrickEmpty) set_mip(k, BrickRef{});
+      return;
+    case kLeaf: {
+      ssize = std::min<uint32_t>(sat_u32(nb.size) / dim, dim * 2);
+      for (int a = 0; a < 3; ++a)
+        start[a] = round_u32(std::floor((float)((up[a] - up[a] % ssize) * 2 * dim) / nb.size));
+      break;
+    }
+    default:
+      if (dominant_bottom) {
+        ssize = sat_u32(nb.size) / dim;
+        for (int a = 0; a < 3; ++a) start[a] = up[a] - up[a] % ssize;
+      } else {
+        ssize = 2;
+        const float mn[3] = {nb.x, nb.y, nb.z};
+        for (int a = 0; a < 3; ++a) {
+          const uint32_t v = round_u32(std::floor(((float)up[a] - mn[a]) * 2.0f * (float)dim / nb.size));
+          start[a] = v - v % 2;
+        }
+      }
+  }
+  uint32_t color = 0;
+  bool sampled = false;
+  if (kind[k] == kLeaf || dominant_bottom) {
+    sampled = mip_resample(sampler, start, ssize, [&](uint32_t x, uint32_t y, uint32_t z, uint32_t* c) {
+      const uint32_t p[3] = {x, y, z};
+      const Entry e = get_internal(k, nb, p);
+      if (!(e.kind & 1u)) return false;
+      *c = e.rgba;
+      return true;
+    }, &color);
+  } else {
+    const float D = (float)dim;
+    if (child(k, octant_of((float)start[0], (float)start[1], (float)start[2], D)) != kEmpty32) {
+      sampled = mip_resample(sampler, start, ssize, [&](uint32_t x, uint32_t y, uint32_t z, uint32_t* c) {
+        const uint8_t o = octant_of((float)x, (float)y, (float)z, D);
+        const uint64_t ck = child(k, o);
+        if (ck == kEmpty32) return false;
+        const uint32_t q[3] = {x - round_u32(off_x(o) * D), y - round_u32(off_y(o) * D), z - round_u32(off_z(o) * D)};
+        const BrickRef& m = mip(ck);
+        uint32_t p;
+        if (m.kind == kBrickEmpty) return false;
+        if (m.kind == kBrickSolid) {
+          p = m.v;
+        } else {
+          const uint64_t fi = flat3(q[0], q[1], q[2], dim);
+          if (fi >= arena.len()) throw ReferencePanic("MIP brick index out of bounds");
+          p = arena.at(m.v)[fi];
+        }
+        const Entry e = pix_entry(p);
+        if (!(e.kind & 1u)) return false;
+        *c = e.rgba;
+        return true;
+      }, &color);
+    }
+  }
+  if (!sampled) return;
+  // the MIP entry: a similar palette colour, or the colour added to the palette (:519-545)
+  uint32_t entry = kEmpty32;
+  const float* thr = nullptr;
+  for (const auto& e : mip_color_thr)
+    if (e.first == level) thr = &e.second;
+  bool similar = false;
+  if (thr) {
+    const float limit = *thr * 255.0f;
+    for (size_t i = 0; i < colors.size(); ++i)
+      if (albedo_distance(color, colors[i]) < limit) {
+        entry = (uint32_t)(uint16_t)i | (kEmpty16 << 16);  // pix_visual
+        similar = true;
+        break;
+      }
+  }
+  if (!similar) {
+    Entry e;
+    e.kind = 1;
+    e.rgba = color;
+    entry = add_to_palette(e);
+  }
+  uint64_t mi[3];
+  matrix_index(nb, up, dim, mi);
+  const uint64_t fi = flat3(mi[0], mi[1], mi[2], dim);
+  BrickRef& m = mip(k);
+  if (fi >= arena.len()) throw ReferencePanic("MIP brick index out of bounds");
+  if (m.kind == kBrickParted) {
+    arena.at(m.v)[fi] = entry;
+    arena.mark(m.v);
+  } else {
+    const uint32_t slot = arena.alloc_fill(m.kind == kBrickSolid ? m.v : kEmpty32);
+    arena.at(slot)[fi] = entry;
+    set_mip(k, BrickRef{kBrickParted, slot});
+  }
+  touch(k);
+}
+
+// StrategyUpdater::recalculate_mip (mipmap.rs:882-899)
+void HostOctree::recalculate_mip(size_t k, const Cube& b) {
+  if (!mips_enabled) return;
+  const float D = (float)dim;
+  for (uint32_t x = 0; x < dim; ++x)
+    for (uint32_t y = 0; y < dim; ++y)
+      for (uint32_t z = 0; z < dim; ++z) {
+        const uint32_t p[3] = {round_u32(b.x + std::round((float)x * b.size / D)),
+                               round_u32(b.y + std::round((float)y * b.size / D)),
+                               round_u32(b.z + std::round((float)z * b.size / D))};
+        update_mip(k, b, p);
+      }
+}
+
+// StrategyUpdater::recalculate_mips (mipmap.rs:798-856)
+void HostOctree::recalculate_mips() {
+  for (BrickRef& m : mips)
+    if (m.kind == kBrickParted) arena.release(m.v);
+  mips.assign(nodes(), BrickRef{});
+  std::fill(node_dirty.begin(), node_dirty.end(), 1);
+  struct Frame {
+    size_t key;
+    Cube b;
+    uint32_t octant;
+  };
+  std::vector<Frame> st{{0, Cube{0.0f, 0.0f, 0.0f, (float)size}, 0}};
+  while (!st.empty()) {
+    Frame& top = st.back();
+    if (top.octant == 8) {
+      const Frame done = top;
+      recalculate_mip(done.key, done.b);
+      st.pop_back();
+      if (!st.empty()) st.back().octant += 1;
+      continue;
+    }
+    check_key(top.key);
+    if (kind[top.key] == kNothing) throw ReferencePanic("BFS shouldn't evaluate empty children");
+    if (kind[top.key] == kInternal) {
+      const uint64_t ck = child(top.key, (uint8_t)top.octant);
+      if (key_valid(ck) && kind[ck] != kNothing) {
+        const float h = top.b.size / 2.0f;
+        const uint8_t o = (uint8_t)top.octant;
+        const Frame next{(size_t)ck, Cube{top.b.x + off_x(o) * h, top.b.y + off_y(o) * h, top.b.z + off_z(o) * h, h}, 0};
+        st.push_back(next);
+      } else {
+        top.octant += 1;
+      }
+    } else {
+      top.octant = 8;
+    }
+  }
+}
+
+// StrategyUpdater::switch_albedo_mip_maps (mipmap.rs:858-880)
+void HostOctree::switch_albedo_mip_maps(bool enabled) {
+  const bool before = mips_enabled;
+  mips_enabled = enabled;
+  if (mips_enabled && before != enabled && kind[0] != kNothing) recalculate_mips();
+}
+
+void HostOctree::set_mip_method(uint32_t level, uint32_t method, float thr) {
+  if (method >= kMipPosterize) thr = std::min(std::max(thr, 0.0f), 1.0f);  // set_method_at_internal
+  for (auto& e : mip_methods)
+    if (e.first == level) {
+      e.second = MipSampler{method, thr};
+      return;
+    }
+  mip_methods.push_back({level, MipSampler{method, thr}});
+}
+
+void HostOctree::set_mip_color_threshold(uint32_t level, float thr) {
+  thr = std::min(std::max(thr, 0.0f), 1.0f);  // set_color_similarity_thr_internal
+  for (auto& e : mip_color_thr)
+    if (e.first == level) {
+      e.second = thr;
+      return;
+    }
+  mip_color_thr.push_back({level, thr});
+}
+
+// StrategyUpdater::sample_root_mip (mipmap.rs:905-937)
+Entry HostOctree::sample_root_mip(uint8_t octant, const uint32_t p[3]) {
+  const uint64_t key = octant == 8 ? 0 : child(0, octant);
+  if (!key_valid(key)) return Entry{};
+  const BrickRef& m = mip(key);
+  if (m.kind == kBrickEmpty) return Entry{};
+  if (m.kind == kBrickSolid) return pix_entry(m.v);
+  const uint64_t fi = flat3(p[0], p[1], p[2], dim);
+  if (fi >= arena.len()) throw ReferencePanic("MIP brick index out of bounds");
+  return pix_entry(arena.at(m.v)[fi]);
+}
+
 // Canonical per-node record (same layout as the oracle's orc_node_record).
 void HostOctree::node_record(uint64_t key, uint64_t rec[40]) const {
   std::memset(rec, 0, sizeof(uint64_t) * 40);
@@ -1267,6 +1595,24 @@ void HostOctree::node_record(uint64_t key, uint64_t rec[40]) const {
           h *= 1099511628211ull;
         }
       rec[29 + i] = h ^ arena.len();
+    }
+  }
+  // the node's MIP brick: kind (numbered like the bricks, 3 = past node_mips), solid value, hash
+  if (key >= mips.size()) {
+    rec[37] = 3;
+  } else {
+    const BrickRef& m = mips[key];
+    rec[37] = m.kind == kBrickEmpty ? 0 : (m.kind == kBrickParted ? 1 : 2);
+    rec[38] = m.kind == kBrickSolid ? m.v : 0;
+    if (m.kind == kBrickParted) {
+      uint64_t h = 1469598103934665603ull;
+      const uint32_t* v = arena.at(m.v);
+      for (uint32_t j = 0; j < arena.len(); ++j)
+        for (int s = 0; s < 4; ++s) {
+          h ^= (v[j] >> (8 * s)) & 0xFFu;
+          h *= 1099511628211ull;
+        }
+      rec[39] = h ^ arena.len();
     }
   }
 }

@@ -89,6 +89,18 @@ class HostOctree {
   Entry get(const uint32_t pos[3]);
   void node_record(uint64_t key, uint64_t rec[40]) const;
 
+  // --- MIP maps (src/octree/mipmap.rs) ---
+  enum MipMethod : uint32_t { kMipBox = 0, kMipPoint = 1, kMipPointBD = 2, kMipPosterize = 3, kMipPosterizeBD = 4 };
+  struct MipSampler {
+    uint32_t method;
+    float thr;
+  };
+  void switch_albedo_mip_maps(bool enabled);
+  void set_mip_method(uint32_t level, uint32_t method, float thr);
+  void set_mip_color_threshold(uint32_t level, float thr);
+  void recalculate_mips();
+  Entry sample_root_mip(uint8_t octant, const uint32_t pos[3]);
+
   // --- state (read by the device image builder) ---
   uint32_t size = 0, dim = 0;
   bool auto_simplify = true;
@@ -104,6 +116,12 @@ class HostOctree {
   std::vector<uint8_t> node_dirty;
   uint64_t colors_synced = 0, datas_synced = 0;
   bool structure_grew = true;
+  // node_mips: one brick per node key, as long as the reference's vector (which is resized beside
+  // most, not all, node pushes); Parted MIP bricks live in the arena
+  bool mips_enabled = false;
+  std::vector<BrickRef> mips;
+  std::vector<std::pair<uint32_t, MipSampler>> mip_methods;  // level -> sampler
+  std::vector<std::pair<uint32_t, float>> mip_color_thr;     // level -> colour matching threshold
 
   bool pix_empty(uint32_t p) const;
   uint64_t stored_occupied_bits(size_t k) const;
@@ -172,6 +190,19 @@ class HostOctree {
   size_t leaf_update(bool overwrite, size_t k, const Cube& node_b, const Cube& target_b, size_t target_octant,
                      const uint32_t pos[3], uint32_t size, uint32_t target_content);
   bool simplify(uint64_t k);
+
+  // MIP maps
+  Entry get_internal(size_t k, Cube cb, const uint32_t pos[3]);
+  void mips_resize() {
+    if (mips.size() < nodes()) mips.resize(nodes());
+  }
+  BrickRef& mip(size_t k) {
+    if (k >= mips.size()) throw ReferencePanic("node_mips index out of bounds");
+    return mips[k];
+  }
+  void set_mip(size_t k, BrickRef b);
+  void update_mip(size_t k, const Cube& b, const uint32_t pos[3]);
+  void recalculate_mip(size_t k, const Cube& b);
 };
 
 }  // namespace svo

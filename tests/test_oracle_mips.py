@@ -53,10 +53,11 @@ def test_mixed_mip_lvl2_where_dim_is_2(oracle_mod):  # tests.rs:278-356
 
 
 def check_dim4(t):
-    assert albedo_of(t.mip_sample_root(0, (0, 0, 0))) == RG
-    assert albedo_of(t.mip_sample_root(1, (0, 0, 0))) == RGB
-    assert albedo_of(t.mip_sample_root(OOB, (0, 0, 0))) == RG
-    assert albedo_of(t.mip_sample_root(OOB, (2, 0, 0))) == RGB
+    sample = t.mip_sample_root if hasattr(t, "mip_sample_root") else t.sample_root_mip  # oracle / product
+    assert albedo_of(sample(0, (0, 0, 0))) == RG
+    assert albedo_of(sample(1, (0, 0, 0))) == RGB
+    assert albedo_of(sample(OOB, (0, 0, 0))) == RG
+    assert albedo_of(sample(OOB, (2, 0, 0))) == RGB
 
 
 def test_mixed_mip_lvl2_where_dim_is_4(oracle_mod):  # tests.rs:358-470
@@ -108,3 +109,86 @@ def test_lod_cast_reads_mips(oracle_mod):
     assert full["status"][0] == 1 and full["brick_octant"][0] != 8
     near = t.cast(origin, direction, viewing_distance=1.0)
     assert near["status"][0] == 1 and near["brick_octant"][0] == 8 and near["albedo"][0] == RG
+
+
+# ---- the product's host octree against the same known answers and the oracle's records ----
+def product_tree(size, dim, voxels, methods=(1,), mips_first=True):
+    import shocovox_gb300 as svo
+    t = svo.Octree(size, dim)
+    t.set_auto_simplify(False)
+    if mips_first:
+        t.switch_albedo_mip_maps(True)
+        for level in methods:
+            t.set_mip_method(level, svo.Octree.BOX_FILTER)
+    for p, c in voxels:
+        t.insert(p, albedo=c)
+    return t
+
+
+def test_product_mips_match_reference_known_answers():
+    assert albedo_of(product_tree(2, 1, MIXED6).sample_root_mip(OOB, (0, 0, 0))) == RG
+    assert albedo_of(product_tree(4, 2, MIXED6).sample_root_mip(OOB, (0, 0, 0))) == RG
+    check_dim4(product_tree(16, 4, MIXED6 + SECOND6, methods=(1, 2)))
+    import shocovox_gb300 as svo
+    t = product_tree(16, 4, MIXED6 + SECOND6, mips_first=False)
+    t.switch_albedo_mip_maps(True)
+    t.set_mip_method(1, svo.Octree.BOX_FILTER).set_mip_method(2, svo.Octree.BOX_FILTER).recalculate_mips()
+    check_dim4(t)
+
+
+def test_product_mip_records_equal_the_oracle(oracle_mod):
+    # random scenes with MIPs enabled before and after construction, every filter, inserts and clears
+    import shocovox_gb300 as svo
+    from helpers import ops_from, INSERT, CLEAR, INSERT_AT_LOD, ALBEDO
+    rng = np.random.default_rng(11)
+    for case in range(24):
+        size, dim = [(16, 2), (32, 4), (64, 4), (32, 8)][case % 4]
+        method = case % 5
+        early = case % 2 == 0
+        ops = []
+        for _ in range(int(rng.integers(40, 200))):
+            x, y, z = (int(v) for v in rng.integers(0, size, 3))
+            r = rng.random()
+            col = int(rng.choice([0xFF0000FF, 0x00FF00FF, 0x0000FFFF, 0x808080FF, 0x102030FF, 0xF0E0D0FF]))
+            if r < 0.75:
+                ops.append((INSERT, x, y, z, ALBEDO, col, 0, 1))
+            elif r < 0.85:
+                s = int(rng.choice([2, 4]))
+                ops.append((INSERT_AT_LOD, x - x % s, y - y % s, z - z % s, ALBEDO, col, 0, s))
+            else:
+                ops.append((CLEAR, x, y, z, 0, 0, 0, 1))
+        ops = ops_from(ops)
+        o = oracle_mod.Tree(size, dim)
+        p = svo.Octree(size, dim)
+        if early:
+            o.mip_switch(True)
+            p.switch_albedo_mip_maps(True)
+        for level in (1, 2, 3):
+            o.mip_set_method(level, method, 0.3)
+            p.set_mip_method(level, method, 0.3)
+        # both stop at the same operation where the reference would panic (e.g. a MIP of a node
+        # pushed where the reference does not grow node_mips)
+        assert apply_status(o, ops) == apply_status(p, ops), "case %d" % case
+        if not early:
+            assert switch_status(o) == switch_status(p), "case %d" % case
+        assert o.records() == p.records(), "case %d" % case
+        assert list(o.palette(0)) == list(p.palette(0)), "case %d" % case
+
+
+def apply_status(t, ops):
+    import re
+    try:
+        t.apply_ops(ops)
+        return (0, len(ops))
+    except Exception as e:  # OracleError / OctreeError: status code and the operation it stopped at
+        code = getattr(e, "code", None)
+        at = int(re.search(r"op (\d+)", str(e)).group(1))
+        return (code, at)
+
+
+def switch_status(t):
+    try:
+        t.mip_switch(True) if hasattr(t, "mip_switch") else t.switch_albedo_mip_maps(True)
+        return 0
+    except Exception as e:
+        return getattr(e, "code", -1)
