@@ -175,6 +175,12 @@ svo_status svo_scene_release_device(svo_scene* scene);
  * overlap.  A CUDA graph that captured a cast reuses the counter of the stream it was captured
  * on: do not run it concurrently with casts on that stream. */
 svo_status svo_cast(svo_scene* scene, const svo_rays* rays, uint64_t n, const svo_hits* hits, void* stream);
+/* Octree::get_by_ray_at_lod (raytracing_on_cpu.rs:325-565): with MIP maps enabled (svo_mip_switch) a
+ * node's MIP brick is read once its level is below (origin - p rounded to the level's grid).length()
+ * / viewing_distance; a hit on a MIP brick reports brick_octant 8.  Without MIP maps this is
+ * svo_cast.  Device buffers; the MIP form runs one thread per ray. */
+svo_status svo_cast_lod(svo_scene* scene, const svo_rays* rays, uint64_t n, const svo_hits* hits, float viewing_distance,
+                        void* stream);
 /* Same cast with host (ideally pinned) ray and hit buffers: host->device copy,
  * cast, device->host copy, stream synchronised before return.  Uses a
  * per-scene device workspace that grows on demand. */

@@ -139,6 +139,12 @@ class Octree:
         h = Hits(**{k: _vp(hits.get(k, 0) or 0) for k in HIT_FIELDS})
         check(lib().svo_cast(self._h, ctypes.byref(r), n, ctypes.byref(h), _vp(stream)))
 
+    def cast_lod(self, rays, hits, n, viewing_distance, stream=0):
+        """get_by_ray_at_lod on device buffers (dicts of device pointers, like cast())."""
+        r = Rays(*[_vp(rays[k]) for k in ("ox", "oy", "oz", "dx", "dy", "dz")])
+        h = Hits(**{k: _vp(hits.get(k, 0) or 0) for k in HIT_FIELDS})
+        check(lib().svo_cast_lod(self._h, ctypes.byref(r), n, ctypes.byref(h), viewing_distance, _vp(stream)))
+
     def cast_host(self, origins, directions, fields=tuple(HIT_FIELDS), stream=0):
         """Host-buffer cast (copies in, casts, copies out, synchronises)."""
         o = np.ascontiguousarray(np.asarray(origins, dtype=np.float32).reshape(-1, 3))

@@ -241,9 +241,11 @@ __device__ __forceinline__ void fill_shared_luts(SharedLuts& L) {
 }
 
 // Octree::get_by_ray (raytracing_on_cpu.rs:316-565, MIP maps disabled)
-template <bool kCount, bool kFast>
+// kLod: get_by_ray_at_lod with MIP maps enabled (s.mips), reading a node's MIP brick when its
+// level is below the one the travelled distance asks for (:366-386).
+template <bool kCount, bool kFast, bool kLod = false>
 __device__ void cast_ray(const SceneView& s, const SharedLuts& L, float ox, float oy, float oz, float dx, float dy,
-                         float dz, HitRecord& h) {
+                         float dz, HitRecord& h, float viewing_distance = 0.0f) {
   h.status = 0;
   h.octant = 0;
   h.node = 0;
@@ -284,6 +286,7 @@ __device__ void cast_ray(const SceneView& s, const SharedLuts& L, float ox, floa
     target = hash_region(r.px - 0.0f, r.py - 0.0f, r.pz - 0.0f, S * 0.5f);
   }
   uint32_t work = 0;
+  float mip_level = s.mip_top;  // (:350) kept across restarts
   while (target != kOob) {
     uint32_t cur = 0;
     cb = Bounds{0.0f, 0.0f, 0.0f, S, s.inv_size};
@@ -301,6 +304,25 @@ __device__ void cast_ray(const SceneView& s, const SharedLuts& L, float ox, floa
       const uint32_t meta = head.z;
       const uint32_t kind = meta & 3u;
       bool backtrack = kind == kKindUniform;
+      if (kLod && s.mips) {
+        // mip_level < (origin - round(p / (2 mip_level)) * 2 mip_level).length() / viewing_distance
+        const float m2 = mip_level * 2.0f;
+        const float ax = ox - roundf(r.px / m2) * m2, ay = oy - roundf(r.py / m2) * m2, az = oz - roundf(r.pz / m2) * m2;
+        if (mip_level < sqrtf((ax * ax + ay * ay) + az * az) / viewing_distance) {
+          const uint32_t mk = (meta >> 24) & 3u;
+          if (mk == 3u) {  // node_mips[key] past the vector: the reference panics
+            h.status = 3;
+            return;
+          }
+          const uint32_t rc = probe_brick<kCount, kFast>(s, r, mk, head.w, cb, h, work);
+          if (rc) {
+            h.status = rc;
+            h.node = cur;
+            h.octant = 8;  // the node's MIP brick
+            return;
+          }
+        }
+      }
       if (target != kOob) {
         if (kind == kKindUniform) {
           const uint32_t rc = probe_brick<kCount, kFast>(s, r, (meta >> 8) & 3u, __ldg(&nd->slot[0]), cb, h, work);
@@ -336,6 +358,7 @@ __device__ void cast_ray(const SceneView& s, const SharedLuts& L, float ox, floa
         s1 = s2;
         s2 = s3;
         --count;
+        if (kLod) mip_level += 1.0f;
         if (count > 0) {
           cur = s0;
           // min - fmod(min, 2s): bounds minima are non-negative multiples of s and 2s is a power of
@@ -363,6 +386,7 @@ __device__ void cast_ray(const SceneView& s, const SharedLuts& L, float ox, floa
         s1 = s0;
         s0 = ck;
         count = count < 4 ? count + 1 : 4;
+        if (kLod) mip_level -= 1.0f;
       } else {
         // ADVANCE (:494-544)
         float bx = rclamp(rx, kTol, 4.0f - kTol);

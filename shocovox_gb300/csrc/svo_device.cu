@@ -86,6 +86,22 @@ svo_status create_queues(DeviceImage& d) {
   return SVO_OK;
 }
 
+// get_by_ray_at_lod with MIP maps enabled: the literal form of the cast with MIP reads, one thread per ray.
+template <bool kCount>
+__global__ void __launch_bounds__(128) lod_kernel(SceneView s, RaysView rays, HitsView out, uint64_t n,
+                                                  float viewing_distance) {
+  __shared__ SharedLuts L;
+  fill_shared_luts(L);
+  __syncthreads();
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  HitRecord h;
+  cast_ray<kCount, false, true>(s, L, __ldg(rays.ox + i), __ldg(rays.oy + i), __ldg(rays.oz + i), __ldg(rays.dx + i),
+                                __ldg(rays.dy + i), __ldg(rays.dz + i), h, viewing_distance);
+  write_hit(s, out, i, h);
+  if (kCount) write_counters(out, i, h);
+}
+
 int g_cast_mode = 0;
 
 // ------------------------------------------------------------------ device image
@@ -121,6 +137,10 @@ SceneView scene_view(const svo_scene* sc) {
   v.inv_size = 1.0f / v.size;
   v.inv_dim = 1.0f / (float)v.dim;
   v.literal = g_cast_mode == 1 ? 1u : 0u;
+  v.mips = sc->tree.mips_enabled ? 1u : 0u;
+  uint32_t levels = 0;
+  for (uint32_t r = sc->tree.size / sc->tree.dim; r > 1; r >>= 1) ++levels;
+  v.mip_top = (float)levels;
   return v;
 }
 
@@ -148,6 +168,13 @@ void build_node(const HostOctree& t, size_t k, DevNode& n) {
       n.meta |= (uint32_t)b.kind << (8 + 2 * i);
       n.slot[i] = b.kind == kBrickEmpty ? 0u : b.v;
     }
+  }
+  if (k >= t.mips.size()) {
+    n.meta |= 3u << 24;
+  } else {
+    const BrickRef& m = t.mips[k];
+    n.meta |= (uint32_t)m.kind << 24;
+    n.mip = m.kind == kBrickEmpty ? 0u : m.v;
   }
 }
 
@@ -484,6 +511,28 @@ svo_status svo_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_h
   if (n && (!rays->ox || !rays->oy || !rays->oz || !rays->dx || !rays->dy || !rays->dz))
     return fail(SVO_ERR_ARGUMENT, "svo_cast: NULL ray array");
   return launch_cast(sc, rays, n, hits, (cudaStream_t)stream);
+}
+
+svo_status svo_cast_lod(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_hits* hits, float viewing_distance,
+                        void* stream) {
+  if (!sc || !rays || !hits) return fail(SVO_ERR_ARGUMENT, "NULL argument");
+  if (!sc->dev.valid) return fail(SVO_ERR_NOT_UPLOADED, "svo_cast_lod: scene not uploaded");
+  if (n == 0) return SVO_OK;
+  if (!rays->ox || !rays->oy || !rays->oz || !rays->dx || !rays->dy || !rays->dz)
+    return fail(SVO_ERR_ARGUMENT, "svo_cast_lod: NULL ray array");
+  const cudaStream_t st = (cudaStream_t)stream;
+  // without MIP maps get_by_ray_at_lod is get_by_ray
+  if (!sc->tree.mips_enabled) return launch_cast(sc, rays, n, hits, st);
+  const uint64_t grid = (n + 127) / 128;
+  if (grid > 0x7FFFFFFFull) return fail(SVO_ERR_ARGUMENT, "svo_cast_lod: too many rays for one launch");
+  const SceneView v = scene_view(sc);
+  const RaysView rv{rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz};
+  if (counts_requested(*hits))
+    lod_kernel<true><<<(unsigned)grid, 128, 0, st>>>(v, rv, hits_view_of(*hits), n, viewing_distance);
+  else
+    lod_kernel<false><<<(unsigned)grid, 128, 0, st>>>(v, rv, hits_view_of(*hits), n, viewing_distance);
+  SVO_CUDA_TRY(cudaGetLastError());
+  return SVO_OK;
 }
 
 svo_status svo_cast_host(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_hits* hits, void* stream) {

@@ -15,8 +15,9 @@ namespace svo {
 // reads one 32-byte sector for (ocbits, meta) and one for the 8 slots.
 struct alignas(64) DevNode {
   uint64_t ocbits;   // stored_occupied_bits (src/octree/detail.rs:508-528)
-  uint32_t meta;     // [1:0] content kind, [2] reserved, [23:8] 2-bit brick kind per octant
-  uint32_t pad0;
+  uint32_t meta;     // [1:0] content kind, [2] reserved, [23:8] 2-bit brick kind per octant,
+                     // [25:24] MIP brick kind (3: the key has no node_mips entry)
+  uint32_t mip;      // the node's MIP brick: Solid value or arena slot
   uint32_t pad1[4];
   uint32_t slot[8];  // Internal: child key or kInvalidChild; Leaf: brick per octant; UniformLeaf: slot[0]
 };
@@ -46,6 +47,8 @@ struct SceneView {
   float inv_size;   // 1 / size (exact: a power of two)
   float inv_dim;    // 1 / D (exact: a power of two)
   uint32_t literal; // 1: every ray takes the literal form of the cast (diagnostics)
+  uint32_t mips;    // MIP maps enabled (get_by_ray_at_lod reads node MIPs)
+  float mip_top;    // log2(size / D): the MIP level the LOD cast starts at (an integer)
 };
 
 // Cast form selected by svo_set_cast_mode (0 automatic, 1 literal only).

@@ -194,6 +194,7 @@ class HostOctree {
   // MIP maps
   Entry get_internal(size_t k, Cube cb, const uint32_t pos[3]);
   void mips_resize() {
+    for (size_t k = mips.size(); k < nodes(); ++k) touch(k);  // their device records gain an entry
     if (mips.size() < nodes()) mips.resize(nodes());
   }
   BrickRef& mip(size_t k) {
