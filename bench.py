@@ -40,6 +40,10 @@ WORKLOADS = {
                            rays=("sphere", 1 << 22)),
     "multiscene64": dict(multi=64, seed=0x5EED0004),
     "served16": dict(served=16, seed=0x5EED0005, rate=2000.0, requests=600, budget_gb=60.0),
+    # terrain512 with MIP maps, cast through get_by_ray_at_lod at a viewing distance of 256
+    "lod512": dict(lod=256.0, kind=1, size=512, brick_dim=8, seed=0x5EED0002, spheres=0, octaves=3,
+                   base_freq=1.0 / 128, height_lo=0.02 * S_TERRAIN, height_hi=0.33 * S_TERRAIN, cave_threshold=0.55,
+                   rays=("cameras", 4, 1920, 1080, 70.0)),
     # the terrain512 scene seen through examples/cpu_render.rs's viewport: fused ray generation + cast + shading
     "viewport512": dict(viewport=4, kind=1, size=512, brick_dim=8, seed=0x5EED0002, spheres=0, octaves=3,
                         base_freq=1.0 / 128, height_lo=0.02 * S_TERRAIN, height_hi=0.33 * S_TERRAIN,
@@ -682,6 +686,120 @@ def run_viewport(args, w):
     }))
 
 
+def run_lod(args, w):
+    """get_by_ray_at_lod with MIP maps (svo_cast_lod) on the terrain512 scene and cameras."""
+    import torch
+    import shocovox_gb300 as svo
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    t0 = time.perf_counter()
+    ops = scene_ops(svo, w)
+    scene = svo.Octree(w["size"], w["brick_dim"])
+    scene.apply_ops(ops)
+    build_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    scene.switch_albedo_mip_maps(True)  # recalculate_mips with the default strategy
+    mip_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream(dev)
+    s = stream.cuda_stream
+    scene.upload(s)
+    origins, dirs = make_rays(svo, w)
+    n = len(origins)
+    cols = [np.ascontiguousarray(origins[:, i]) for i in range(3)] + [np.ascontiguousarray(dirs[:, i]) for i in range(3)]
+    rays = {k: torch.from_numpy(c).to(dev) for k, c in zip(("ox", "oy", "oz", "dx", "dy", "dz"), cols)}
+    rp = {k: v.data_ptr() for k, v in rays.items()}
+    tmap = {np.uint8: torch.uint8, np.uint32: torch.int32, np.float32: torch.float32}
+    out = {k: torch.empty(n, dtype=tmap[svo.HIT_FIELDS[k]], device=dev) for k in OUT_FIELDS}
+    hp = {k: v.data_ptr() for k, v in out.items()}
+    vd = w["lod"]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    ms = timed(lambda: scene.cast_lod(rp, hp, n, vd, s))
+    max_ms = timed(lambda: scene.cast_lod(rp, hp, n, float(np.finfo(np.float32).max), s))
+    plain_ms = timed(lambda: scene.cast(rp, hp, n, s))
+    # end to end: rays from pinned host memory, status + albedo back, copies in the timed region
+    pin_in = {k: torch.from_numpy(c).pin_memory() for k, c in zip(("ox", "oy", "oz", "dx", "dy", "dz"), cols)}
+    pin_out = {k: torch.empty(n, dtype=tmap[svo.HIT_FIELDS[k]]).pin_memory() for k in ("status", "albedo")}
+
+    def e2e():
+        for k, v in pin_in.items():
+            rays[k].copy_(v, non_blocking=True)
+        scene.cast_lod(rp, hp, n, vd, s)
+        for k, v in pin_out.items():
+            v.copy_(out[k], non_blocking=True)
+    e2e()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t1) / args.steps
+    clk = clocks.stop()
+    cnt = {k: torch.empty(n, dtype=torch.int32, device=dev) for k in COUNTERS}
+    st = torch.empty(n, dtype=torch.uint8, device=dev)
+    oct_ = torch.empty(n, dtype=torch.uint8, device=dev)
+    scene.cast_lod(rp, dict(status=st.data_ptr(), brick_octant=oct_.data_ptr(), **{k: v.data_ptr() for k, v in cnt.items()}),
+                   n, vd, s)
+    torch.cuda.synchronize()
+    visits, creads, vreads, runs = (int(cnt[k].to(torch.int64).sum()) for k in COUNTERS)
+    hits = int((st == 1).sum())
+    mip_hits = int(((st == 1) & (oct_ == 8)).sum())
+    alg = alg_bytes_of(visits - runs, creads, vreads, hits)
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle
+        ot = oracle.Tree(w["size"], w["brick_dim"])
+        ot.apply_ops(ops)
+        ot.mip_switch(True)
+        threads = os.cpu_count() or 1
+        step = max(1, n // 400000)
+        so, sd = np.ascontiguousarray(origins[::step]), np.ascontiguousarray(dirs[::step])
+        tt = time.perf_counter()
+        ot.cast(so, sd, threads=threads, viewing_distance=vd)
+        dt = time.perf_counter() - tt
+        cpu = {"value": round(len(so) / dt / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": "every %dth ray of the batch (%d rays, %.1fs on %d threads)" % (step, len(so), dt, threads)}
+    peak, peak_src = measured_peak()
+    achieved = alg / (ms / 1e3) / 1e9
+    st_ = scene.stats()
+    print(json.dumps({
+        "metric": "Mrays/s", "value": round(n / (ms / 1e3) / 1e6, 3), "unit": "Mrays/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "lod512", "octree": "%d^3" % w["size"], "brick_dim": w["brick_dim"],
+                   "rays_per_step": n, "viewing_distance": vd, "hit_rate": round(hits / n, 4),
+                   "mip_hit_rate": round(mip_hits / n, 4), "build_s": round(build_s, 1),
+                   "mip_recalculation_s": round(mip_s, 1), "nodes": st_["nodes"],
+                   "per_ray": {"node_visits": round(visits / n, 2), "child_reads": round(creads / n, 2),
+                               "voxel_reads": round(vreads / n, 2)},
+                   "l2": "inputs larger than L2 (rays %.0f MB + hits %.0f MB per step)" % (
+                       n * 24 / 1e6, n * sum(OUT_BYTES.values()) / 1e6),
+                   "lod_at_f32_max": {"value": round(n / (max_ms / 1e3) / 1e6, 3), "ms_per_step": round(max_ms, 4)},
+                   "svo_cast_same_rays": {"value": round(n / (plain_ms / 1e3) / 1e6, 3),
+                                          "ms_per_step": round(plain_ms, 4)}},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_src,
+                     "alg_bytes_per_launch": alg, "alg_bytes_per_ray": round(alg / n, 2)},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(n / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": n * 24,
+                "d2h_bytes_per_step": n * 5},
+        "gpu_launches": args.steps, "clocks": clk,
+    }))
+
+
 def run_reference(args, w):
     rank, _, world = dist_env()
     if rank != 0:
@@ -734,7 +852,7 @@ def main():
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
-        if "multi" in w or "served" in w or "viewport" in w:
+        if "multi" in w or "served" in w or "viewport" in w or "lod" in w:
             print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the default single-scene workload"}))
             return
         run_reference(args, w)
@@ -747,6 +865,9 @@ def main():
         return
     if "viewport" in w:
         run_viewport(args, w)
+        return
+    if "lod" in w:
+        run_lod(args, w)
         return
 
     rank, local_rank, world = dist_env()
@@ -832,6 +953,18 @@ def main():
         scene.cast_host_soa(cols_np, out_np, s)
     e2e_s = max_over_ranks(time.perf_counter() - t0, pg)
     e2e_value = n * world * args.steps / e2e_s / 1e6
+    # the two ways svo_cast_host can move the data (svo_set_host_transfer), each timed the same way
+    e2e_paths = {}
+    for mode, name in ((1, "staged_copies"), (2, "direct_host_access")):
+        if svo.lib().svo_set_host_transfer(mode) != 0:
+            e2e_paths[name] = None
+            continue
+        scene.cast_host_soa(cols_np, out_np, s)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            scene.cast_host_soa(cols_np, out_np, s)
+        e2e_paths[name] = round(n * world * args.steps / max_over_ranks(time.perf_counter() - t0, pg) / 1e6, 3)
+    svo.lib().svo_set_host_transfer(0)
 
     cpu = None
     if want_cpu:
@@ -874,7 +1007,7 @@ def main():
                          "alg_bytes_per_ray": round(alg_bytes / n, 2), "l2": l2},
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": n * 24,
-                    "d2h_bytes_per_step": n * sum(OUT_BYTES.values())},
+                    "d2h_bytes_per_step": n * sum(OUT_BYTES.values()), "paths": e2e_paths},
             "gpu_launches": args.steps,
             "clocks": clk,
             "variants": variants,

@@ -44,7 +44,8 @@ enum {
   SVO_ERR_OUT_OF_MEMORY = 9,       /* device allocation failed */
   SVO_ERR_BUDGET = 10,             /* a server admission exceeds its device-memory budget */
   SVO_ERR_NOT_FOUND = 11,          /* unknown server scene / request id */
-  SVO_ERR_BUSY = 12                /* request queue full or a result not ready yet */
+  SVO_ERR_BUSY = 12,               /* request queue full or a result not ready yet */
+  SVO_ERR_IO = 13                  /* a file could not be opened, read or written */
 };
 
 /* Per-ray status codes written by the cast. */
@@ -129,6 +130,16 @@ svo_status svo_apply_ops(svo_scene* scene, const svo_op* ops, uint64_t n, uint64
 /* Octree::get (src/octree/mod.rs:416-422) */
 svo_status svo_get(svo_scene* scene, uint32_t x, uint32_t y, uint32_t z, uint32_t* kind, uint32_t* rgba, uint32_t* user);
 svo_status svo_scene_stats_get(svo_scene* scene, svo_scene_stats* out);
+
+/* ---- persistence: Octree::to_bytes / from_bytes / save / load (src/octree/mod.rs:138-168) in the
+ *      reference's bencode bytecode format (src/convert/bytecode.rs) ---------------------------- */
+/* Serialises the octree (node pool, children, MIPs, palettes, MIP strategy); with out NULL only
+ * *length is set. */
+svo_status svo_scene_to_bytes(svo_scene* scene, uint8_t* out, uint64_t capacity, uint64_t* length);
+/* A new scene from serialised bytes (no device image yet). */
+svo_status svo_scene_from_bytes(const uint8_t* bytes, uint64_t length, svo_scene** out);
+svo_status svo_scene_save(svo_scene* scene, const char* path);
+svo_status svo_scene_load(const char* path, svo_scene** out);
 
 /* ---- MIP maps: the StrategyUpdater of Octree::albedo_mip_map_resampling_strategy()
  *      (src/octree/mipmap.rs:609-880; disabled by default) ---------------------------- */
@@ -330,6 +341,11 @@ svo_status svo_selftest_luts(uint64_t* ray_to_node, uint32_t* octant_step, uint6
  * restatement otherwise; 1 the literal restatement for every ray.  Both give the
  * same results; mode 1 exists so tests can check that. */
 svo_status svo_set_cast_mode(int32_t mode);
+/* How svo_cast_host moves rays and hits (process-wide): 0 (default) lets the kernel read and write
+ * the host buffers in place when the device accesses host memory through the CPU's page tables
+ * (Grace systems) and stages copies elsewhere; 1 always stages copies (chunks over three streams);
+ * 2 always accesses host memory directly (an error where the device cannot). */
+svo_status svo_set_host_transfer(int32_t mode);
 
 #ifdef __cplusplus
 }

@@ -9,6 +9,7 @@ kernels behind the C ABI in include/svo.h); this module only marshals
 arguments.  There is no CPU fallback: without libsvo nothing here works.
 """
 import ctypes
+import os
 
 import numpy as np
 
@@ -58,6 +59,37 @@ class Octree:
         if h:
             lib().svo_scene_destroy(h)
             self._h = None
+
+    @classmethod
+    def _adopt(cls, h):
+        t = cls.__new__(cls)
+        t._h = h
+        st = t.stats()
+        t.size, t.brick_dim = st["size"], st["brick_dim"]
+        return t
+
+    # ---- persistence: Octree::to_bytes / from_bytes / save / load (src/octree/mod.rs:138-168) ----
+    def to_bytes(self):
+        n = ctypes.c_uint64()
+        check(lib().svo_scene_to_bytes(self._h, None, 0, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(max(n.value, 1))
+        check(lib().svo_scene_to_bytes(self._h, buf, n.value, ctypes.byref(n)))
+        return buf.raw[:n.value]
+
+    @classmethod
+    def from_bytes(cls, data):
+        h = ctypes.c_void_p()
+        check(lib().svo_scene_from_bytes(data, len(data), ctypes.byref(h)))
+        return cls._adopt(h)
+
+    def save(self, path):
+        check(lib().svo_scene_save(self._h, os.fsencode(path)))
+
+    @classmethod
+    def load(cls, path):
+        h = ctypes.c_void_p()
+        check(lib().svo_scene_load(os.fsencode(path), ctypes.byref(h)))
+        return cls._adopt(h)
 
     @property
     def handle(self):

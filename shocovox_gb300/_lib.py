@@ -100,6 +100,10 @@ SIGNATURES = {
     "svo_get": (_I32, [_VP, _U32, _U32, _U32, _P(_U32), _P(_U32), _P(_U32)]),
     "svo_scene_stats_get": (_I32, [_VP, _P(SceneStats)]),
     "svo_node_record": (_I32, [_VP, _U64, _P(_U64)]),
+    "svo_scene_to_bytes": (_I32, [_VP, _VP, _U64, _P(_U64)]),
+    "svo_scene_from_bytes": (_I32, [_VP, _U64, _P(_VP)]),
+    "svo_scene_save": (_I32, [_VP, ctypes.c_char_p]),
+    "svo_scene_load": (_I32, [ctypes.c_char_p, _P(_VP)]),
     "svo_mip_switch": (_I32, [_VP, _I32]),
     "svo_mip_set_method": (_I32, [_VP, _U32, _U32, ctypes.c_float]),
     "svo_mip_set_color_threshold": (_I32, [_VP, _U32, ctypes.c_float]),
@@ -129,6 +133,7 @@ SIGNATURES = {
     "svo_gen_sphere_rays": (_I32, [_P(_F), _F, _U64, _U64, _VP, _VP, _VP, _VP, _VP, _VP]),
     "svo_selftest_luts": (_I32, [_P(_U64), _P(_U32), _P(_U64)]),
     "svo_set_cast_mode": (_I32, [_I32]),
+    "svo_set_host_transfer": (_I32, [_I32]),
 }
 
 

@@ -3,6 +3,8 @@
 // SVO_ERR_REFERENCE_PANIC, allocation failure SVO_ERR_OUT_OF_MEMORY.
 #include <cstring>
 #include <new>
+#include <cstdio>
+#include <memory>
 #include <string>
 
 #include "svo_internal.h"
@@ -70,6 +72,63 @@ svo_status svo_set_auto_simplify(svo_scene* s, int32_t enabled) {
   if (!s) return fail(SVO_ERR_ARGUMENT, "NULL scene");
   s->tree.auto_simplify = enabled != 0;
   return SVO_OK;
+}
+
+// ---- persistence: Octree::to_bytes / from_bytes / save / load (src/octree/mod.rs:138-168) ----
+svo_status svo_scene_to_bytes(svo_scene* s, uint8_t* out, uint64_t capacity, uint64_t* length) {
+  if (!s || !length) return fail(SVO_ERR_ARGUMENT, "NULL argument");
+  return guarded("svo_scene_to_bytes", [&]() -> svo_status {
+    std::string bytes;
+    s->tree.encode(bytes);
+    *length = bytes.size();
+    if (!out) return SVO_OK;
+    if (capacity < bytes.size()) return fail(SVO_ERR_ARGUMENT, "svo_scene_to_bytes: buffer too small");
+    std::memcpy(out, bytes.data(), bytes.size());
+    return SVO_OK;
+  });
+}
+
+svo_status svo_scene_from_bytes(const uint8_t* bytes, uint64_t length, svo_scene** out) {
+  if (!out || (!bytes && length)) return fail(SVO_ERR_ARGUMENT, "NULL argument");
+  *out = nullptr;
+  return guarded("svo_scene_from_bytes", [&]() -> svo_status {
+    std::unique_ptr<svo_scene> s(new svo_scene());
+    std::string err;
+    const int rc = HostOctree::decode(bytes, (size_t)length, &s->tree, &err);
+    if (rc != 0) return err.empty() ? op_status(rc, "Octree::from_bytes") : fail((svo_status)rc, "svo_scene_from_bytes: " + err);
+    *out = s.release();
+    return SVO_OK;
+  });
+}
+
+svo_status svo_scene_save(svo_scene* s, const char* path) {
+  if (!s || !path) return fail(SVO_ERR_ARGUMENT, "NULL argument");
+  return guarded("svo_scene_save", [&]() -> svo_status {
+    std::string bytes;
+    s->tree.encode(bytes);
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(SVO_ERR_IO, std::string("svo_scene_save: cannot open ") + path);
+    const bool ok = std::fwrite(bytes.data(), 1, bytes.size(), f) == bytes.size();
+    if (std::fclose(f) != 0 || !ok) return fail(SVO_ERR_IO, std::string("svo_scene_save: cannot write ") + path);
+    return SVO_OK;
+  });
+}
+
+svo_status svo_scene_load(const char* path, svo_scene** out) {
+  if (!path || !out) return fail(SVO_ERR_ARGUMENT, "NULL argument");
+  *out = nullptr;
+  std::string bytes;
+  {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(SVO_ERR_IO, std::string("svo_scene_load: cannot open ") + path);
+    char buf[1 << 16];
+    size_t n;
+    while ((n = std::fread(buf, 1, sizeof(buf), f)) > 0) bytes.append(buf, n);
+    const bool err = std::ferror(f) != 0;
+    std::fclose(f);
+    if (err) return fail(SVO_ERR_IO, std::string("svo_scene_load: cannot read ") + path);
+  }
+  return svo_scene_from_bytes(reinterpret_cast<const uint8_t*>(bytes.data()), bytes.size(), out);
 }
 
 // ---- MIP maps: Octree::albedo_mip_map_resampling_strategy() (src/octree/mipmap.rs) ----

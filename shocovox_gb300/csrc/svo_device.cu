@@ -103,6 +103,7 @@ __global__ void __launch_bounds__(128) lod_kernel(SceneView s, RaysView rays, Hi
 }
 
 int g_cast_mode = 0;
+int g_host_transfer = 0;  // svo_set_host_transfer: 0 auto, 1 staged copies, 2 direct access
 
 // ------------------------------------------------------------------ device image
 uint64_t device_image_bytes(const svo_scene* sc) {
@@ -541,7 +542,29 @@ svo_status svo_cast_host(svo_scene* sc, const svo_rays* rays, uint64_t n, const 
   if (n == 0) return SVO_OK;
   if (!rays->ox || !rays->oy || !rays->oz || !rays->dx || !rays->dy || !rays->dz)
     return fail(SVO_ERR_ARGUMENT, "svo_cast_host: NULL ray array");
-  return cast_host_pipelined(sc, rays, n, hits, (cudaStream_t)stream);
+  const cudaStream_t st = (cudaStream_t)stream;
+  // Where the device reads host memory through the CPU's page tables (Grace: NVLink-C2C with
+  // address translation), the kernel reads the rays and writes the hits in place; elsewhere the
+  // batch goes through staged copies.
+  int direct = 0;
+  if (g_host_transfer != 1) {
+    int dev = 0;
+    SVO_CUDA_TRY(cudaGetDevice(&dev));
+    SVO_CUDA_TRY(cudaDeviceGetAttribute(&direct, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev));
+    if (g_host_transfer == 2 && !direct)
+      return fail(SVO_ERR_ARGUMENT, "svo_cast_host: this device cannot access host memory directly");
+  }
+  if (!direct) return cast_host_pipelined(sc, rays, n, hits, st);
+  const svo_status rc = launch_cast(sc, rays, n, hits, st);
+  if (rc != SVO_OK) return rc;
+  SVO_CUDA_TRY(cudaStreamSynchronize(st));
+  return SVO_OK;
+}
+
+svo_status svo_set_host_transfer(int32_t mode) {
+  if (mode < 0 || mode > 2) return fail(SVO_ERR_ARGUMENT, "svo_set_host_transfer: mode must be 0, 1 or 2");
+  g_host_transfer = mode;
+  return SVO_OK;
 }
 
 svo_status svo_set_cast_mode(int32_t mode) {

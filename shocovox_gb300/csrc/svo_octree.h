@@ -101,6 +101,11 @@ class HostOctree {
   void recalculate_mips();
   Entry sample_root_mip(uint8_t octant, const uint32_t pos[3]);
 
+  // --- persistence: Octree::to_bytes / from_bytes (src/octree/mod.rs:138-168, src/convert/bytecode.rs) ---
+  void encode(std::string& out) const;
+  // returns an svo_status code; `t` must be default-constructed
+  static int decode(const uint8_t* bytes, size_t length, HostOctree* t, std::string* error);
+
   // --- state (read by the device image builder) ---
   uint32_t size = 0, dim = 0;
   bool auto_simplify = true;
