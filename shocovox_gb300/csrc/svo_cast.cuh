@@ -428,6 +428,36 @@ __device__ void cast_ray(const SceneView& s, const SharedLuts& L, float ox, floa
   }
 }
 
+
+// The MIP condition of get_by_ray_at_lod (:366-375): level < (origin - round(p / 2 level) * 2 level).length()
+// / viewing_distance, in the reference's f32 operations.
+__device__ __forceinline__ bool lod_reads_mip(float ox, float oy, float oz, float px, float py, float pz, float level,
+                                              float viewing_distance) {
+  const float m2 = level * 2.0f;
+  const float ax = ox - roundf(px / m2) * m2, ay = oy - roundf(py / m2) * m2, az = oz - roundf(pz / m2) * m2;
+  return level < sqrtf((ax * ax + ay * ay) + az * az) / viewing_distance;
+}
+
+// True when no restart visit from the next one on can read a MIP: the visit after j nudges has
+// level L + j - 1 (L > 0, each visit POPs) and point p_j with |o - p_j| <= |o - p| + j g, g = |c| plus
+// the rounding of one nudge, and the grid point it is rounded to lies within sqrt(3) (level +
+// 2^-22 |p|) of p_j, so the condition is false while (L + j - 1)(vd - sqrt(3)) exceeds
+// |o - p| + j g + sqrt(3) 2^-21 S, padded by 2^-20 for the f32 evaluation.  Both sides grow
+// linearly in j, so the first visit and the slopes decide.  Evaluated in f64.
+static __device__ __noinline__ bool lod_runs_clear(float ox, float oy, float oz, float px, float py, float pz, float cx,
+                                            float cy, float cz, float level, float viewing_distance, float S) {
+  if (!(level > 0.0f) || !(viewing_distance > 0.0f)) return false;
+  const double pad = 1.0 + 0x1p-20, r3 = 1.7320508075688772 * pad;
+  const double vd = (double)viewing_distance, L = (double)level;
+  const double dx = (double)ox - px, dy = (double)oy - py, dz = (double)oz - pz;
+  const double d0 = sqrt(dx * dx + dy * dy + dz * dz) * pad;
+  const double g = sqrt((double)cx * cx + (double)cy * cy + (double)cz * cz) * pad + 0x1p-22 * S * r3;
+  const double slack = r3 * 0x1p-21 * S + 1e-6;
+  if ((vd - r3) < g * pad) return false;                  // the right-hand side could catch up
+  return L * (vd - r3) >= (d0 + g + slack) * pad;         // the first visit (j = 1)
+}
+
+
 // restart_cells_run out of line: it runs a few times per ray at most, and inlined it would add to
 // the register allocation of the whole traversal loop.
 struct RestartRun {
@@ -552,9 +582,20 @@ __device__ __forceinline__ uint32_t probe_brick_fast(const SceneView& s, FastRay
   }
 }
 
+// probe of a node's MIP brick (kind in meta[25:24]; kind 3: no node_mips entry, where the reference panics)
 template <bool kCount>
+__device__ __forceinline__ uint32_t probe_mip(const SceneView& s, FastRay& r, uint32_t meta, uint32_t value,
+                                              const Bounds& b, HitRecord& h, uint32_t& work) {
+  const uint32_t mk = (meta >> 24) & 3u;
+  if (mk == 3u) return 3;
+  return probe_brick_fast<kCount>(s, r, mk, value, b, h, work);
+}
+
+// kLod: get_by_ray_at_lod with MIP maps (s.mips): the MIP reads of the literal form, and restart
+// runs taken in closed form only where lod_runs_clear proves that none of their visits reads a MIP.
+template <bool kCount, bool kLod = false>
 __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox, float oy, float oz, float dx,
-                              float dy, float dz, HitRecord& h) {
+                              float dy, float dz, HitRecord& h, float viewing_distance = 0.0f) {
   h.status = 0;
   h.octant = 0;
   h.node = 0;
@@ -608,6 +649,8 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
     r.fz = sqrtf((e * e + 1.0f) + f * f);
   }
   uint32_t work = 0;
+  float mip_level = s.mip_top;  // (:350) kept across restarts
+  const bool lod = kLod && s.mips;
   while (target != kOob) {
     uint32_t cur = 0;
     cb = Bounds{0.0f, 0.0f, 0.0f, S, s.inv_size};
@@ -626,6 +669,15 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
       const uint32_t kind = meta & 3u;
       const bool uniform = kind == kKindUniform;
       const bool backtrack = uniform;  // a UniformLeaf is always left after its probe
+      if (lod && lod_reads_mip(ox, oy, oz, r.px, r.py, r.pz, mip_level, viewing_distance)) {
+        const uint32_t rc = probe_mip<kCount>(s, r, meta, head.w, cb, h, work);
+        if (rc) {
+          h.status = rc;
+          h.node = cur;
+          h.octant = 8;  // the node's MIP brick
+          return;
+        }
+      }
       if (target != kOob && (uniform || kind == kKindLeaf)) {
         // probe the UniformLeaf's brick over the node bounds, or the Leaf's brick under target_octant
         const uint32_t slot = uniform ? 0u : target;
@@ -658,6 +710,7 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
         s2 = s3;
         oct >>= 3;
         --count;
+        if (kLod) mip_level += 1.0f;
         if (count > 0) {
           cur = s0;
           const float pmx = (ho & 1u) ? cb.x - cb.s : cb.x;
@@ -683,6 +736,7 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
         s1 = s0;
         s0 = ck;
         count = count < 4 ? count + 1 : 4;
+        if (kLod) mip_level -= 1.0f;
       } else {
         // ADVANCE
         float bx = rclamp(rx, kTol, 4.0f - kTol);
@@ -727,6 +781,9 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
     const bool root_runs = (root.z & 3u) == kKindInternal || (root.z & 3u) == kKindNothing;
     const float q4r = s.inv_size * 4.0f;
     while (root_runs && r.px < S && r.py < S && r.pz < S && r.px > 0.0f && r.py > 0.0f && r.pz > 0.0f) {
+      // a root visit that reads the root's MIP (which may move the point before the occupancy
+      // test) is left to the traversal loop
+      if (lod && lod_reads_mip(ox, oy, oz, r.px, r.py, r.pz, mip_level, viewing_distance)) break;
       const float rx = (r.px - 0.0f) * q4r, ry = (r.py - 0.0f) * q4r, rz = (r.pz - 0.0f) * q4r;
       const uint32_t flat = min(__float2uint_rz(rx), 3u) + 4u * min(__float2uint_rz(ry), 3u) +
                             16u * min(__float2uint_rz(rz), 3u);
@@ -736,6 +793,14 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
         return;
       }
       if (kCount) h.visits++;
+      if (kLod) mip_level += 1.0f;  // the root's POP
+      if (lod && !lod_runs_clear(ox, oy, oz, r.px, r.py, r.pz, c01x, c01y, c01z, mip_level, viewing_distance, S)) {
+        // a later restart visit may read the root's MIP: one restart at a time
+        r.px = r.px + c01x;
+        r.py = r.py + c01y;
+        r.pz = r.pz + c01z;
+        continue;
+      }
       // When every axis moves the way the direction octant of the LUT says (only a negative
       // component so small that 1 + d rounds to 1 breaks this), every later cell lies inside this
       // cell's box towards the far corner, whose occupancy bits are empty: all later root tests fail
@@ -769,6 +834,7 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
         return;
       }
       work += k - 1u;
+      if (kLod) mip_level += (float)(k - 1u);  // the skipped visits' POPs
       if (kCount) {
         h.visits += k - 1u;
         h.runs += k - 1u;
@@ -788,12 +854,22 @@ __device__ __noinline__ void cast_ray_literal(const SceneView& s, const SharedLu
   cast_ray<kCount, false>(s, L, ox, oy, oz, dx, dy, dz, h);
 }
 
-// One ray: the exact fast form when the direction holds no NaN, the literal form otherwise.
+// get_by_ray_at_lod for rays whose direction holds a NaN, out of line like cast_ray_literal.
 template <bool kCount>
+__device__ __noinline__ void cast_ray_literal_lod(const SceneView& s, const SharedLuts& L, float ox, float oy, float oz,
+                                                  float dx, float dy, float dz, HitRecord& h, float viewing_distance) {
+  cast_ray<kCount, false, true>(s, L, ox, oy, oz, dx, dy, dz, h, viewing_distance);
+}
+
+// One ray: the exact fast form when the direction holds no NaN, the literal form otherwise; kLod
+// casts get_by_ray_at_lod at the viewing distance.
+template <bool kCount, bool kLod = false>
 __device__ __forceinline__ void cast_one(const SceneView& s, const SharedLuts& L, float ox, float oy, float oz,
-                                         float dx, float dy, float dz, HitRecord& h) {
+                                         float dx, float dy, float dz, HitRecord& h, float viewing_distance = 0.0f) {
   if (!s.literal && !isnan(dx) && !isnan(dy) && !isnan(dz))
-    cast_ray_fast<kCount>(s, L, ox, oy, oz, dx, dy, dz, h);
+    cast_ray_fast<kCount, kLod>(s, L, ox, oy, oz, dx, dy, dz, h, viewing_distance);
+  else if (kLod)
+    cast_ray_literal_lod<kCount>(s, L, ox, oy, oz, dx, dy, dz, h, viewing_distance);
   else
     cast_ray_literal<kCount>(s, L, ox, oy, oz, dx, dy, dz, h);
 }

@@ -35,9 +35,10 @@ __global__ void __launch_bounds__(128, 7) cast_kernel(SceneView s, RaysView rays
 // counter.  The cost of a ray varies by orders of magnitude (a sky ray leaves after a few node
 // visits, a grazing ray walks a whole cave), and a warp that finishes early takes more work
 // instead of idling until its block's slowest warp is done.  The counter starts at 0.
-template <bool kCount>
+template <bool kCount, bool kLod = false>
 __global__ void __launch_bounds__(128, 7)
-    queue_kernel(SceneView s, RaysView rays, HitsView out, uint64_t n, unsigned long long* __restrict__ counter) {
+    queue_kernel(SceneView s, RaysView rays, HitsView out, uint64_t n, unsigned long long* __restrict__ counter,
+                 float viewing_distance = 0.0f) {
   __shared__ SharedLuts L;
   fill_shared_luts(L);
   __syncthreads();
@@ -50,8 +51,8 @@ __global__ void __launch_bounds__(128, 7)
     const uint64_t i = base + lane;
     if (i >= n) continue;
     HitRecord h;
-    cast_one<kCount>(s, L, __ldg(rays.ox + i), __ldg(rays.oy + i), __ldg(rays.oz + i), __ldg(rays.dx + i),
-                     __ldg(rays.dy + i), __ldg(rays.dz + i), h);
+    cast_one<kCount, kLod>(s, L, __ldg(rays.ox + i), __ldg(rays.oy + i), __ldg(rays.oz + i), __ldg(rays.dx + i),
+                     __ldg(rays.dy + i), __ldg(rays.dz + i), h, viewing_distance);
     write_hit(s, out, i, h);
     if (kCount) write_counters(out, i, h);
   }
@@ -86,18 +87,18 @@ svo_status create_queues(DeviceImage& d) {
   return SVO_OK;
 }
 
-// get_by_ray_at_lod with MIP maps enabled: the literal form of the cast with MIP reads, one thread per ray.
+// get_by_ray_at_lod one thread per ray, for streams without a work counter.
 template <bool kCount>
-__global__ void __launch_bounds__(128) lod_kernel(SceneView s, RaysView rays, HitsView out, uint64_t n,
-                                                  float viewing_distance) {
+__global__ void __launch_bounds__(128) lod_grid_kernel(SceneView s, RaysView rays, HitsView out, uint64_t n,
+                                                       float viewing_distance) {
   __shared__ SharedLuts L;
   fill_shared_luts(L);
   __syncthreads();
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   HitRecord h;
-  cast_ray<kCount, false, true>(s, L, __ldg(rays.ox + i), __ldg(rays.oy + i), __ldg(rays.oz + i), __ldg(rays.dx + i),
-                                __ldg(rays.dy + i), __ldg(rays.dz + i), h, viewing_distance);
+  cast_one<kCount, true>(s, L, __ldg(rays.ox + i), __ldg(rays.oy + i), __ldg(rays.oz + i), __ldg(rays.dx + i),
+                         __ldg(rays.dy + i), __ldg(rays.dz + i), h, viewing_distance);
   write_hit(s, out, i, h);
   if (kCount) write_counters(out, i, h);
 }
@@ -524,14 +525,33 @@ svo_status svo_cast_lod(svo_scene* sc, const svo_rays* rays, uint64_t n, const s
   const cudaStream_t st = (cudaStream_t)stream;
   // without MIP maps get_by_ray_at_lod is get_by_ray
   if (!sc->tree.mips_enabled) return launch_cast(sc, rays, n, hits, st);
-  const uint64_t grid = (n + 127) / 128;
-  if (grid > 0x7FFFFFFFull) return fail(SVO_ERR_ARGUMENT, "svo_cast_lod: too many rays for one launch");
+  CastQueues* q = sc->dev.queues;
   const SceneView v = scene_view(sc);
   const RaysView rv{rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz};
-  if (counts_requested(*hits))
-    lod_kernel<true><<<(unsigned)grid, 128, 0, st>>>(v, rv, hits_view_of(*hits), n, viewing_distance);
+  const HitsView hv = hits_view_of(*hits);
+  const bool count = counts_requested(*hits);
+  std::lock_guard<std::mutex> lock(q->m);
+  unsigned long long* ctr = queue_counter(q, st);
+  if (!ctr) {
+    const uint64_t blocks = (n + 127) / 128;
+    if (blocks > 0x7FFFFFFFull) return fail(SVO_ERR_ARGUMENT, "svo_cast_lod: too many rays for one launch");
+    if (count)
+      lod_grid_kernel<true><<<(unsigned)blocks, 128, 0, st>>>(v, rv, hv, n, viewing_distance);
+    else
+      lod_grid_kernel<false><<<(unsigned)blocks, 128, 0, st>>>(v, rv, hv, n, viewing_distance);
+    SVO_CUDA_TRY(cudaGetLastError());
+    return SVO_OK;
+  }
+  static const int per_sm_lod[2] = {  // resident blocks of the two LOD queue kernels
+      [] { int v = 0; return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, queue_kernel<false, true>, 128, 0) == cudaSuccess ? v : 1; }(),
+      [] { int v = 0; return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, queue_kernel<true, true>, 128, 0) == cudaSuccess ? v : 1; }()};
+  const int per_sm = std::max(1, per_sm_lod[count ? 1 : 0]);
+  const uint64_t grid = std::min<uint64_t>((uint64_t)q->sm_count * per_sm, (n + 127) / 128);
+  SVO_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st));
+  if (count)
+    queue_kernel<true, true><<<(unsigned)grid, 128, 0, st>>>(v, rv, hv, n, ctr, viewing_distance);
   else
-    lod_kernel<false><<<(unsigned)grid, 128, 0, st>>>(v, rv, hits_view_of(*hits), n, viewing_distance);
+    queue_kernel<false, true><<<(unsigned)grid, 128, 0, st>>>(v, rv, hv, n, ctr, viewing_distance);
   SVO_CUDA_TRY(cudaGetLastError());
   return SVO_OK;
 }
