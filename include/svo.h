@@ -141,6 +141,20 @@ svo_status svo_scene_from_bytes(const uint8_t* bytes, uint64_t length, svo_scene
 svo_status svo_scene_save(svo_scene* scene, const char* path);
 svo_status svo_scene_load(const char* path, svo_scene** out);
 
+/* ---- MagicaVoxel .vox import (src/convert/magicavoxel.rs) -------------------------------- */
+/* Octree::load_vox_file (magicavoxel.rs:258-276): a new scene of size 2^ceil(log2(extent)) holding
+ * every voxel of frame 0 of the file's scene graph, inserted in file order as its palette colour. */
+svo_status svo_scene_from_vox(const uint8_t* bytes, uint64_t length, uint32_t brick_dim, svo_scene** out);
+svo_status svo_scene_load_vox(const char* path, uint32_t brick_dim, svo_scene** out);
+/* The two halves of MIPMapStrategy::load_vox_file (magicavoxel.rs:204-241), which sets the MIP
+ * strategy between them: the octree size the file asks for, and the insertion of its voxels into
+ * a scene (load_vox_data_internal, magicavoxel.rs:337-385). */
+svo_status svo_vox_tree_size(const uint8_t* bytes, uint64_t length, uint32_t* size);
+svo_status svo_vox_insert(svo_scene* scene, const uint8_t* bytes, uint64_t length);
+/* parse_rotation_matrix (magicavoxel.rs:61-90): the 3x3 row-major matrix of a rotation byte;
+ * SVO_ERR_REFERENCE_PANIC where the reference indexes past the matrix. */
+svo_status svo_vox_rotation(uint8_t byte, int8_t out[9]);
+
 /* ---- MIP maps: the StrategyUpdater of Octree::albedo_mip_map_resampling_strategy()
  *      (src/octree/mipmap.rs:609-880; disabled by default) ---------------------------- */
 typedef enum {

@@ -91,6 +91,45 @@ class Octree:
         check(lib().svo_scene_load(os.fsencode(path), ctypes.byref(h)))
         return cls._adopt(h)
 
+    # ---- MagicaVoxel import: Octree::load_vox_file / MIPMapStrategy::load_vox_file
+    #      (src/convert/magicavoxel.rs:204-385) ----
+    @classmethod
+    def from_vox(cls, data, brick_dim, configure=None):
+        """The octree of a .vox file's frame 0. With `configure` (a callable taking the new, still
+        empty octree, e.g. to set its MIP strategy) the size is taken from the file, `configure`
+        runs, then the voxels are inserted: MIPMapStrategy::load_vox_file."""
+        data = bytes(data)
+        if configure is None:
+            h = ctypes.c_void_p()
+            check(lib().svo_scene_from_vox(data, len(data), brick_dim, ctypes.byref(h)))
+            return cls._adopt(h)
+        t = cls(cls.vox_tree_size(data), brick_dim)
+        configure(t)
+        check(lib().svo_vox_insert(t._h, data, len(data)))
+        return t
+
+    @classmethod
+    def load_vox(cls, path, brick_dim, configure=None):
+        if configure is None:
+            h = ctypes.c_void_p()
+            check(lib().svo_scene_load_vox(os.fsencode(path), brick_dim, ctypes.byref(h)))
+            return cls._adopt(h)
+        with open(path, "rb") as f:
+            return cls.from_vox(f.read(), brick_dim, configure)
+
+    @staticmethod
+    def vox_tree_size(data):
+        n = ctypes.c_uint32()
+        check(lib().svo_vox_tree_size(bytes(data), len(data), ctypes.byref(n)))
+        return n.value
+
+    @staticmethod
+    def vox_rotation(byte):
+        """parse_rotation_matrix: the row-major 3x3 matrix of a .vox rotation byte."""
+        m = (ctypes.c_int8 * 9)()
+        check(lib().svo_vox_rotation(byte, m))
+        return [list(m[0:3]), list(m[3:6]), list(m[6:9])]
+
     @property
     def handle(self):
         return self._h

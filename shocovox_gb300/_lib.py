@@ -104,6 +104,11 @@ SIGNATURES = {
     "svo_scene_from_bytes": (_I32, [_VP, _U64, _P(_VP)]),
     "svo_scene_save": (_I32, [_VP, ctypes.c_char_p]),
     "svo_scene_load": (_I32, [ctypes.c_char_p, _P(_VP)]),
+    "svo_scene_from_vox": (_I32, [_VP, _U64, _U32, _P(_VP)]),
+    "svo_scene_load_vox": (_I32, [ctypes.c_char_p, _U32, _P(_VP)]),
+    "svo_vox_tree_size": (_I32, [_VP, _U64, _P(_U32)]),
+    "svo_vox_insert": (_I32, [_VP, _VP, _U64]),
+    "svo_vox_rotation": (_I32, [ctypes.c_uint8, _P(ctypes.c_int8)]),
     "svo_mip_switch": (_I32, [_VP, _I32]),
     "svo_mip_set_method": (_I32, [_VP, _U32, _U32, ctypes.c_float]),
     "svo_mip_set_color_threshold": (_I32, [_VP, _U32, ctypes.c_float]),
