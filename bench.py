@@ -88,6 +88,12 @@ def make_rays(svo, w):
     raise ValueError(spec)
 
 
+def ray_rows(w):
+    """Row length of the workload's rays when they are camera images in raster order, else 0."""
+    spec = w.get("rays", ())
+    return spec[2] if spec and spec[0] in ("cameras", "orbit") else 0
+
+
 def measured_peak():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -192,18 +198,18 @@ def oracle_tree_async(ops, w):
     return th, box
 
 
-def cpu_cast_rate(tree, origins, dirs, target_s, threads):
+def cpu_cast_rate(tree, origins, dirs, target_s, threads, **cast_args):
     """Rays/s of the oracle cast over a strided sample sized for about target_s seconds."""
     n = len(origins)
     probe = max(1, n // 20000)
     t0 = time.perf_counter()
-    tree.cast(origins[::probe], dirs[::probe], threads=threads)
+    tree.cast(origins[::probe], dirs[::probe], threads=threads, **cast_args)
     rate = len(origins[::probe]) / max(time.perf_counter() - t0, 1e-6)
     m = int(min(n, max(20000, rate * target_s)))
     step = max(1, n // m)
     so, sd = origins[::step], dirs[::step]
     t0 = time.perf_counter()
-    tree.cast(so, sd, threads=threads)
+    tree.cast(so, sd, threads=threads, **cast_args)
     dt = time.perf_counter() - t0
     return len(so) / dt, len(so), step, dt
 
@@ -615,11 +621,11 @@ def run_viewport(args, w):
     outs = {k: torch.empty(n, dtype=tmap[svo.HIT_FIELDS[k]], device=dev) for k in ("status", "albedo", "nx", "ny", "nz")}
     hp = {k: v.data_ptr() for k, v in outs.items()}
     for _ in range(args.warmup):
-        scene.cast(rp, hp, n, s)
+        scene.cast(rp, hp, n, s, row_length=W)
     torch.cuda.synchronize()
     e0.record(stream)
     for _ in range(args.steps):
-        scene.cast(rp, hp, n, s)
+        scene.cast(rp, hp, n, s, row_length=W)
     e1.record(stream)
     torch.cuda.synchronize()
     cast_ms = e0.elapsed_time(e1) / args.steps
@@ -629,7 +635,7 @@ def run_viewport(args, w):
     def cast_frames():
         for k in range(len(vps)):
             scene.cast({kk: v + 4 * k * per for kk, v in rp.items()},
-                       {kk: v + (1 if kk == "status" else 4) * k * per for kk, v in hp.items()}, per, s)
+                       {kk: v + (1 if kk == "status" else 4) * k * per for kk, v in hp.items()}, per, s, row_length=W)
     cast_frames()
     torch.cuda.synchronize()
     e0.record(stream)
@@ -640,7 +646,7 @@ def run_viewport(args, w):
     cast_frames_ms = e0.elapsed_time(e1) / args.steps
     cnt = {k: torch.empty(n, dtype=torch.int32, device=dev) for k in COUNTERS}
     st = torch.empty(n, dtype=torch.uint8, device=dev)
-    scene.cast(rp, dict(status=st.data_ptr(), **{k: v.data_ptr() for k, v in cnt.items()}), n, s)
+    scene.cast(rp, dict(status=st.data_ptr(), **{k: v.data_ptr() for k, v in cnt.items()}), n, s, row_length=W)
     torch.cuda.synchronize()
     visits, creads, vreads, runs = (int(cnt[k].to(torch.int64).sum()) for k in COUNTERS)
     hits = int((st == 1).sum())
@@ -725,11 +731,13 @@ def run_lod(args, w):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / args.steps
 
+    row = ray_rows(w)  # camera images in raster order: svo_cast_lod_rows
     clocks = ClockSampler(0)
     clocks.start()
-    ms = timed(lambda: scene.cast_lod(rp, hp, n, vd, s))
-    max_ms = timed(lambda: scene.cast_lod(rp, hp, n, float(np.finfo(np.float32).max), s))
-    plain_ms = timed(lambda: scene.cast(rp, hp, n, s))
+    ms = timed(lambda: scene.cast_lod(rp, hp, n, vd, s, row_length=row))
+    max_ms = timed(lambda: scene.cast_lod(rp, hp, n, float(np.finfo(np.float32).max), s, row_length=row))
+    plain_ms = timed(lambda: scene.cast(rp, hp, n, s, row_length=row))
+    lod_plain_order_ms = timed(lambda: scene.cast_lod(rp, hp, n, vd, s))
     # end to end: rays from pinned host memory, status + albedo back, copies in the timed region
     pin_in = {k: torch.from_numpy(c).pin_memory() for k, c in zip(("ox", "oy", "oz", "dx", "dy", "dz"), cols)}
     pin_out = {k: torch.empty(n, dtype=tmap[svo.HIT_FIELDS[k]]).pin_memory() for k in ("status", "albedo")}
@@ -737,7 +745,7 @@ def run_lod(args, w):
     def e2e():
         for k, v in pin_in.items():
             rays[k].copy_(v, non_blocking=True)
-        scene.cast_lod(rp, hp, n, vd, s)
+        scene.cast_lod(rp, hp, n, vd, s, row_length=row)
         for k, v in pin_out.items():
             v.copy_(out[k], non_blocking=True)
     e2e()
@@ -765,13 +773,9 @@ def run_lod(args, w):
         ot.apply_ops(ops)
         ot.mip_switch(True)
         threads = os.cpu_count() or 1
-        step = max(1, n // 400000)
-        so, sd = np.ascontiguousarray(origins[::step]), np.ascontiguousarray(dirs[::step])
-        tt = time.perf_counter()
-        ot.cast(so, sd, threads=threads, viewing_distance=vd)
-        dt = time.perf_counter() - tt
-        cpu = {"value": round(len(so) / dt / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
-               "sample": "every %dth ray of the batch (%d rays, %.1fs on %d threads)" % (step, len(so), dt, threads)}
+        rate, m, step, dt = cpu_cast_rate(ot, origins, dirs, args.cpu_seconds, threads, viewing_distance=vd)
+        cpu = {"value": round(rate / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": "every %dth ray of the batch (%d rays, %.1fs on %d threads)" % (step, m, dt, threads)}
     peak, peak_src = measured_peak()
     achieved = alg / (ms / 1e3) / 1e9
     st_ = scene.stats()
@@ -789,7 +793,10 @@ def run_lod(args, w):
                        n * 24 / 1e6, n * sum(OUT_BYTES.values()) / 1e6),
                    "lod_at_f32_max": {"value": round(n / (max_ms / 1e3) / 1e6, 3), "ms_per_step": round(max_ms, 4)},
                    "svo_cast_same_rays": {"value": round(n / (plain_ms / 1e3) / 1e6, 3),
-                                          "ms_per_step": round(plain_ms, 4)}},
+                                          "ms_per_step": round(plain_ms, 4)},
+                   "ray_order": "rows of %d rays (svo_cast_lod_rows: 8 x 4 ray blocks per warp)" % row,
+                   "svo_cast_lod_plain_order": {"value": round(n / (lod_plain_order_ms / 1e3) / 1e6, 3),
+                                                "ms_per_step": round(lod_plain_order_ms, 4)}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_src,
                      "alg_bytes_per_launch": alg, "alg_bytes_per_ray": round(alg / n, 2)},
@@ -902,16 +909,18 @@ def main():
     hp = {k: v.data_ptr() for k, v in outs.items()}
     s = stream.cuda_stream
 
+    # camera rays in raster order: svo_cast_rows hands warps 8 x 4 blocks of neighbouring pixels
+    row = ray_rows(w)
     clocks = ClockSampler(local_rank)
     clocks.start()  # samples from the warm-up on, so that short timed regions still get samples
     for _ in range(args.warmup):
-        scene.cast(rp, hp, n, s)
+        scene.cast(rp, hp, n, s, row_length=row)
     torch.cuda.synchronize()
 
     # algorithmic bytes of one launch from the instrumented cast (counters equal the oracle's, see tests)
     cnt = {k: torch.empty(n, dtype=torch.int32, device=dev) for k in COUNTERS}
     st = torch.empty(n, dtype=torch.uint8, device=dev)
-    scene.cast(rp, dict(status=st.data_ptr(), **{k: v.data_ptr() for k, v in cnt.items()}), n, s)
+    scene.cast(rp, dict(status=st.data_ptr(), **{k: v.data_ptr() for k, v in cnt.items()}), n, s, row_length=row)
     torch.cuda.synchronize()
     visits, creads, vreads, runs = (int(cnt[k].to(torch.int64).sum()) for k in COUNTERS)
     hits = int((st == 1).sum())
@@ -924,7 +933,7 @@ def main():
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
-        scene.cast(rp, hp, n, s)
+        scene.cast(rp, hp, n, s, row_length=row)
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
@@ -933,6 +942,19 @@ def main():
     ms = max_over_ranks(ms, pg)
     ms_step = ms / args.steps
     value = n * world / (ms_step / 1e3) / 1e6
+    # the same rays through plain svo_cast (warps take 32 consecutive rays of one row)
+    plain = None
+    if row:
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            scene.cast(rp, hp, n, s)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pms = max_over_ranks(e0.elapsed_time(e1), pg) / args.steps
+        plain = {"value": round(n * world / (pms / 1e3) / 1e6, 3), "ms_per_step": round(pms, 4)}
 
     variants = None
     if not args.no_variants:
@@ -945,12 +967,12 @@ def main():
     cols_np = [c.numpy() for c in pin_cols]
     out_np = {k: v.numpy() for k, v in pin_out.items()}
     for _ in range(max(1, args.warmup)):
-        scene.cast_host_soa(cols_np, out_np, s)
+        scene.cast_host_soa(cols_np, out_np, s, row_length=row)
     if pg:
         pg.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        scene.cast_host_soa(cols_np, out_np, s)
+        scene.cast_host_soa(cols_np, out_np, s, row_length=row)
     e2e_s = max_over_ranks(time.perf_counter() - t0, pg)
     e2e_value = n * world * args.steps / e2e_s / 1e6
     # the two ways svo_cast_host can move the data (svo_set_host_transfer), each timed the same way
@@ -959,10 +981,10 @@ def main():
         if svo.lib().svo_set_host_transfer(mode) != 0:
             e2e_paths[name] = None
             continue
-        scene.cast_host_soa(cols_np, out_np, s)
+        scene.cast_host_soa(cols_np, out_np, s, row_length=row)
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            scene.cast_host_soa(cols_np, out_np, s)
+            scene.cast_host_soa(cols_np, out_np, s, row_length=row)
         e2e_paths[name] = round(n * world * args.steps / max_over_ranks(time.perf_counter() - t0, pg) / 1e6, 3)
     svo.lib().svo_set_host_transfer(0)
 
@@ -1000,7 +1022,10 @@ def main():
                        "l2": "inputs larger than L2 (rays %.0f MB + hits %.0f MB per step); the %.0f MB scene image "
                              "stays resident" % (n * 24 / 1e6, n * sum(OUT_BYTES.values()) / 1e6,
                                                  st["device_bytes"] / 1e6),
-                       "build_s": round(build_s, 1), "parallelism": "replicas" if world > 1 else "single"},
+                       "build_s": round(build_s, 1), "parallelism": "replicas" if world > 1 else "single",
+                       "ray_order": ("rows of %d rays (svo_cast_rows: 8 x 4 ray blocks per warp)" % row) if row
+                       else "as generated (svo_cast)",
+                       "svo_cast_plain_order": plain},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_src,
                          "alg_bytes_per_launch": alg_bytes,

@@ -203,13 +203,26 @@ svo_status svo_cast(svo_scene* scene, const svo_rays* rays, uint64_t n, const sv
 /* Octree::get_by_ray_at_lod (raytracing_on_cpu.rs:325-565): with MIP maps enabled (svo_mip_switch) a
  * node's MIP brick is read once its level is below (origin - p rounded to the level's grid).length()
  * / viewing_distance; a hit on a MIP brick reports brick_octant 8.  Without MIP maps this is
- * svo_cast.  Device buffers; the MIP form runs one thread per ray. */
+ * svo_cast.  Device buffers, the same work queue as svo_cast. */
 svo_status svo_cast_lod(svo_scene* scene, const svo_rays* rays, uint64_t n, const svo_hits* hits, float viewing_distance,
                         void* stream);
-/* Same cast with host (ideally pinned) ray and hit buffers: host->device copy,
- * cast, device->host copy, stream synchronised before return.  Uses a
- * per-scene device workspace that grows on demand. */
+/* Same cast with host ray and hit buffers, stream synchronised before return.  Where the device
+ * reads host memory through the CPU's page tables (Grace) the kernel reads the rays and writes the
+ * hits in place; elsewhere the batch is staged in chunks through a per-scene device workspace that
+ * grows on demand, copies overlapping the casts (with pinned host memory). */
 svo_status svo_cast_host(svo_scene* scene, const svo_rays* rays, uint64_t n, const svo_hits* hits, void* stream);
+/* The three casts above for rays laid out as rows of row_length rays (a camera image in raster
+ * order, or several images one after the other): the work queue hands each warp 8 neighbouring rays
+ * of 4 neighbouring rows instead of 32 rays of one row, so its rays stay in step longer.  Hits are
+ * identical to the plain calls' (rays are independent); row_length 0, or a batch of fewer than 4
+ * rows, casts in plain order.  No counterpart in the reference, whose renderer casts one pixel at a
+ * time (examples/cpu_render.rs:104-138). */
+svo_status svo_cast_rows(svo_scene* scene, const svo_rays* rays, uint64_t n, uint32_t row_length, const svo_hits* hits,
+                         void* stream);
+svo_status svo_cast_lod_rows(svo_scene* scene, const svo_rays* rays, uint64_t n, uint32_t row_length,
+                             const svo_hits* hits, float viewing_distance, void* stream);
+svo_status svo_cast_host_rows(svo_scene* scene, const svo_rays* rays, uint64_t n, uint32_t row_length,
+                              const svo_hits* hits, void* stream);
 
 /* ---- fused viewport render: examples/cpu_render.rs:77-138 on the device ---- */
 /* The example's frame: a viewport of width x height world units at distance fov in front of

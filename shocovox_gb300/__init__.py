@@ -204,19 +204,21 @@ class Octree:
         check(lib().svo_scene_release_device(self._h))
 
     # ---- the cast ----
-    def cast(self, rays, hits, n, stream=0):
-        """Device cast: ``rays`` / ``hits`` map field names to device pointers (ints)."""
+    def cast(self, rays, hits, n, stream=0, row_length=0):
+        """Device cast: ``rays`` / ``hits`` map field names to device pointers (ints). ``row_length``:
+        the rays are rows of that many rays (a camera image in raster order), see svo_cast_rows."""
         r = Rays(*[_vp(rays[k]) for k in ("ox", "oy", "oz", "dx", "dy", "dz")])
         h = Hits(**{k: _vp(hits.get(k, 0) or 0) for k in HIT_FIELDS})
-        check(lib().svo_cast(self._h, ctypes.byref(r), n, ctypes.byref(h), _vp(stream)))
+        check(lib().svo_cast_rows(self._h, ctypes.byref(r), n, row_length, ctypes.byref(h), _vp(stream)))
 
-    def cast_lod(self, rays, hits, n, viewing_distance, stream=0):
+    def cast_lod(self, rays, hits, n, viewing_distance, stream=0, row_length=0):
         """get_by_ray_at_lod on device buffers (dicts of device pointers, like cast())."""
         r = Rays(*[_vp(rays[k]) for k in ("ox", "oy", "oz", "dx", "dy", "dz")])
         h = Hits(**{k: _vp(hits.get(k, 0) or 0) for k in HIT_FIELDS})
-        check(lib().svo_cast_lod(self._h, ctypes.byref(r), n, ctypes.byref(h), viewing_distance, _vp(stream)))
+        check(lib().svo_cast_lod_rows(self._h, ctypes.byref(r), n, row_length, ctypes.byref(h), viewing_distance,
+                                      _vp(stream)))
 
-    def cast_host(self, origins, directions, fields=tuple(HIT_FIELDS), stream=0):
+    def cast_host(self, origins, directions, fields=tuple(HIT_FIELDS), stream=0, row_length=0):
         """Host-buffer cast (copies in, casts, copies out, synchronises)."""
         o = np.ascontiguousarray(np.asarray(origins, dtype=np.float32).reshape(-1, 3))
         d = np.ascontiguousarray(np.asarray(directions, dtype=np.float32).reshape(-1, 3))
@@ -225,15 +227,15 @@ class Octree:
         out = {k: np.zeros(n, dtype=HIT_FIELDS[k]) for k in fields}
         r = Rays(*[_vp(c.ctypes.data) for c in cols])
         h = Hits(**{k: _vp(out[k].ctypes.data) if k in out else None for k in HIT_FIELDS})
-        check(lib().svo_cast_host(self._h, ctypes.byref(r), n, ctypes.byref(h), _vp(stream)))
+        check(lib().svo_cast_host_rows(self._h, ctypes.byref(r), n, row_length, ctypes.byref(h), _vp(stream)))
         return out
 
-    def cast_host_soa(self, cols, out, stream=0):
+    def cast_host_soa(self, cols, out, stream=0, row_length=0):
         """Host cast over caller-owned arrays: cols = 6 float32 arrays, out = {field: array}."""
         n = len(cols[0])
         r = Rays(*[_vp(c.ctypes.data) for c in cols])
         h = Hits(**{k: _vp(out[k].ctypes.data) if k in out else None for k in HIT_FIELDS})
-        check(lib().svo_cast_host(self._h, ctypes.byref(r), n, ctypes.byref(h), _vp(stream)))
+        check(lib().svo_cast_host_rows(self._h, ctypes.byref(r), n, row_length, ctypes.byref(h), _vp(stream)))
 
     # ---- MIP maps: Octree::albedo_mip_map_resampling_strategy() (src/octree/mipmap.rs) ----
     BOX_FILTER, POINT_FILTER, POINT_FILTER_BD, POSTERIZE, POSTERIZE_BD = range(5)

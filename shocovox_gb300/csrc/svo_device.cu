@@ -31,24 +31,59 @@ __global__ void __launch_bounds__(128, 7) cast_kernel(SceneView s, RaysView rays
   if (kCount) write_counters(out, i, h);
 }
 
-// Queued cast: a persistent grid whose warps claim 32 consecutive rays at a time from a work
-// counter.  The cost of a ray varies by orders of magnitude (a sky ray leaves after a few node
-// visits, a grazing ray walks a whole cave), and a warp that finishes early takes more work
-// instead of idling until its block's slowest warp is done.  The counter starts at 0.
+// Which rays a warp's claim covers.  Rays laid out as rows of `row` rays (a camera image, or
+// several stacked) are claimed as blocks of 8 neighbouring rays in 4 neighbouring rows, whose
+// traversals stay in step far longer than 32 rays of one row; the rays past the last full band
+// of 4 rows, and every ray of a batch without a row layout, are claimed 32 consecutive rays at a
+// time.  Any order gives the same hits: rays are independent.
+struct ClaimOrder {
+  uint64_t row = 0;       // rays per row; 0: no row layout
+  uint64_t per_band = 0;  // 8-ray blocks per band of 4 rows
+  uint64_t blocks = 0;    // claims that are blocks
+  uint64_t tail = 0;      // first ray claimed 32 consecutive rays at a time
+  uint64_t claims = 0;    // claims in all
+};
+
+ClaimOrder claim_order(uint64_t n, uint64_t row) {
+  ClaimOrder o;
+  if (row >= 8 && n >= 4 * row) {
+    o.row = row;
+    o.per_band = (row + 7) / 8;
+    o.blocks = (n / (4 * row)) * o.per_band;
+    o.tail = (n / (4 * row)) * 4 * row;
+  }
+  o.claims = o.blocks + (n - o.tail + 31) / 32;
+  return o;
+}
+
+// the ray of `lane` in claim c, or n when the lane has none
+__device__ __forceinline__ uint64_t claimed_ray(const ClaimOrder& o, uint64_t c, uint32_t lane, uint64_t n) {
+  if (c < o.blocks) {
+    const uint64_t band = c / o.per_band, col = (c - band * o.per_band) * 8 + (lane & 7u);
+    return col < o.row ? (band * 4 + (lane >> 3)) * o.row + col : n;
+  }
+  const uint64_t i = o.tail + (c - o.blocks) * 32 + lane;
+  return i < n ? i : n;
+}
+
+// Queued cast: a persistent grid whose warps claim 32 rays at a time from a work counter.  The
+// cost of a ray varies by orders of magnitude (a sky ray leaves after a few node visits, a
+// grazing ray walks a whole cave), and a warp that finishes early takes more work instead of
+// idling until its block's slowest warp is done.  The counter (claims taken) starts at 0.
 template <bool kCount, bool kLod = false>
 __global__ void __launch_bounds__(128, 7)
-    queue_kernel(SceneView s, RaysView rays, HitsView out, uint64_t n, unsigned long long* __restrict__ counter,
-                 float viewing_distance = 0.0f) {
+    queue_kernel(SceneView s, RaysView rays, HitsView out, uint64_t n, ClaimOrder order,
+                 unsigned long long* __restrict__ counter, float viewing_distance = 0.0f) {
   __shared__ SharedLuts L;
   fill_shared_luts(L);
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31u;
   for (;;) {
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(counter, 32ull);
-    base = __shfl_sync(0xFFFFFFFFu, base, 0);
-    if (base >= n) break;
-    const uint64_t i = base + lane;
+    unsigned long long c = 0;
+    if (lane == 0) c = atomicAdd(counter, 1ull);
+    c = __shfl_sync(0xFFFFFFFFu, c, 0);
+    if (c >= order.claims) break;
+    const uint64_t i = claimed_ray(order, c, lane, n);
     if (i >= n) continue;
     HitRecord h;
     cast_one<kCount, kLod>(s, L, __ldg(rays.ox + i), __ldg(rays.oy + i), __ldg(rays.oz + i), __ldg(rays.dx + i),
@@ -321,7 +356,8 @@ svo_status incremental_sync(svo_scene* sc, cudaStream_t st) {
 }
 
 
-svo_status launch_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_hits* hits, cudaStream_t st) {
+svo_status launch_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_hits* hits, cudaStream_t st,
+                       uint64_t row = 0) {
   if (n == 0) return SVO_OK;
   const SceneView v = scene_view(sc);
   RaysView rv{rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz};
@@ -335,10 +371,11 @@ svo_status launch_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const sv
       const int per_sm = std::max(1, count ? q->blocks_per_sm_count : q->blocks_per_sm);
       const uint64_t grid = std::min<uint64_t>((uint64_t)q->sm_count * per_sm, (n + block - 1) / block);
       SVO_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st));
+      const ClaimOrder order = claim_order(n, row);
       if (count)
-        queue_kernel<true><<<(unsigned)grid, block, 0, st>>>(v, rv, hv, n, ctr);
+        queue_kernel<true><<<(unsigned)grid, block, 0, st>>>(v, rv, hv, n, order, ctr);
       else
-        queue_kernel<false><<<(unsigned)grid, block, 0, st>>>(v, rv, hv, n, ctr);
+        queue_kernel<false><<<(unsigned)grid, block, 0, st>>>(v, rv, hv, n, order, ctr);
       SVO_CUDA_TRY(cudaGetLastError());
       return SVO_OK;
     }
@@ -383,13 +420,14 @@ void destroy_pipeline(DeviceImage& d) {
 }
 
 svo_status cast_host_pipelined(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_hits* hits,
-                               cudaStream_t caller) {
+                               cudaStream_t caller, uint64_t row) {
   DeviceImage& d = sc->dev;
   void* const* host_fields = reinterpret_cast<void* const*>(hits);
   size_t per_ray = 24;
   for (int f = 0; f < kHitFields; ++f)
     if (host_fields[f]) per_ray += kHitFieldBytes[f];
-  const uint64_t chunk = std::min<uint64_t>(n, std::max<uint64_t>(262144, ((n / 6 + 255) / 256) * 256));
+  uint64_t chunk = std::min<uint64_t>(n, std::max<uint64_t>(262144, ((n / 6 + 255) / 256) * 256));
+  if (row) chunk = std::min<uint64_t>(n, ((chunk + 4 * row - 1) / (4 * row)) * 4 * row);  // whole bands of rows
   const size_t need = (size_t)chunk * per_ray + 32 * 256;
   HostPipeline* p = static_cast<HostPipeline*>(d.ws);
   if (!p) {
@@ -438,7 +476,7 @@ svo_status cast_host_pipelined(svo_scene* sc, const svo_rays* rays, uint64_t n, 
         o += ((kHitFieldBytes[f] * chunk + 255) / 256) * 256;
       }
     svo_rays drays{dr[0], dr[1], dr[2], dr[3], dr[4], dr[5]};
-    svo_status rc = launch_cast(sc, &drays, m, &dh, st);
+    svo_status rc = launch_cast(sc, &drays, m, &dh, st, row);
     if (rc != SVO_OK) return rc;
     for (int f = 0; f < kHitFields; ++f)
       if (host_fields[f])
@@ -507,16 +545,21 @@ void svo_scene_destroy(svo_scene* sc) {
   delete sc;
 }
 
-svo_status svo_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_hits* hits, void* stream) {
+svo_status svo_cast_rows(svo_scene* sc, const svo_rays* rays, uint64_t n, uint32_t row_length, const svo_hits* hits,
+                         void* stream) {
   if (!sc || !rays || !hits) return fail(SVO_ERR_ARGUMENT, "svo_cast: NULL argument");
   if (!sc->dev.valid) return fail(SVO_ERR_NOT_UPLOADED, "svo_cast: scene has no device image (svo_scene_upload)");
   if (n && (!rays->ox || !rays->oy || !rays->oz || !rays->dx || !rays->dy || !rays->dz))
     return fail(SVO_ERR_ARGUMENT, "svo_cast: NULL ray array");
-  return launch_cast(sc, rays, n, hits, (cudaStream_t)stream);
+  return launch_cast(sc, rays, n, hits, (cudaStream_t)stream, row_length);
 }
 
-svo_status svo_cast_lod(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_hits* hits, float viewing_distance,
-                        void* stream) {
+svo_status svo_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_hits* hits, void* stream) {
+  return svo_cast_rows(sc, rays, n, 0, hits, stream);
+}
+
+svo_status svo_cast_lod_rows(svo_scene* sc, const svo_rays* rays, uint64_t n, uint32_t row, const svo_hits* hits,
+                             float viewing_distance, void* stream) {
   if (!sc || !rays || !hits) return fail(SVO_ERR_ARGUMENT, "NULL argument");
   if (!sc->dev.valid) return fail(SVO_ERR_NOT_UPLOADED, "svo_cast_lod: scene not uploaded");
   if (n == 0) return SVO_OK;
@@ -524,7 +567,7 @@ svo_status svo_cast_lod(svo_scene* sc, const svo_rays* rays, uint64_t n, const s
     return fail(SVO_ERR_ARGUMENT, "svo_cast_lod: NULL ray array");
   const cudaStream_t st = (cudaStream_t)stream;
   // without MIP maps get_by_ray_at_lod is get_by_ray
-  if (!sc->tree.mips_enabled) return launch_cast(sc, rays, n, hits, st);
+  if (!sc->tree.mips_enabled) return launch_cast(sc, rays, n, hits, st, row);
   CastQueues* q = sc->dev.queues;
   const SceneView v = scene_view(sc);
   const RaysView rv{rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz};
@@ -548,15 +591,22 @@ svo_status svo_cast_lod(svo_scene* sc, const svo_rays* rays, uint64_t n, const s
   const int per_sm = std::max(1, per_sm_lod[count ? 1 : 0]);
   const uint64_t grid = std::min<uint64_t>((uint64_t)q->sm_count * per_sm, (n + 127) / 128);
   SVO_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st));
+  const ClaimOrder order = claim_order(n, row);
   if (count)
-    queue_kernel<true, true><<<(unsigned)grid, 128, 0, st>>>(v, rv, hv, n, ctr, viewing_distance);
+    queue_kernel<true, true><<<(unsigned)grid, 128, 0, st>>>(v, rv, hv, n, order, ctr, viewing_distance);
   else
-    queue_kernel<false, true><<<(unsigned)grid, 128, 0, st>>>(v, rv, hv, n, ctr, viewing_distance);
+    queue_kernel<false, true><<<(unsigned)grid, 128, 0, st>>>(v, rv, hv, n, order, ctr, viewing_distance);
   SVO_CUDA_TRY(cudaGetLastError());
   return SVO_OK;
 }
 
-svo_status svo_cast_host(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_hits* hits, void* stream) {
+svo_status svo_cast_lod(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_hits* hits, float viewing_distance,
+                        void* stream) {
+  return svo_cast_lod_rows(sc, rays, n, 0, hits, viewing_distance, stream);
+}
+
+svo_status svo_cast_host_rows(svo_scene* sc, const svo_rays* rays, uint64_t n, uint32_t row_length,
+                              const svo_hits* hits, void* stream) {
   if (!sc || !rays || !hits) return fail(SVO_ERR_ARGUMENT, "svo_cast_host: NULL argument");
   if (!sc->dev.valid) return fail(SVO_ERR_NOT_UPLOADED, "svo_cast_host: scene has no device image");
   if (n == 0) return SVO_OK;
@@ -574,11 +624,15 @@ svo_status svo_cast_host(svo_scene* sc, const svo_rays* rays, uint64_t n, const 
     if (g_host_transfer == 2 && !direct)
       return fail(SVO_ERR_ARGUMENT, "svo_cast_host: this device cannot access host memory directly");
   }
-  if (!direct) return cast_host_pipelined(sc, rays, n, hits, st);
-  const svo_status rc = launch_cast(sc, rays, n, hits, st);
+  if (!direct) return cast_host_pipelined(sc, rays, n, hits, st, row_length);
+  const svo_status rc = launch_cast(sc, rays, n, hits, st, row_length);
   if (rc != SVO_OK) return rc;
   SVO_CUDA_TRY(cudaStreamSynchronize(st));
   return SVO_OK;
+}
+
+svo_status svo_cast_host(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_hits* hits, void* stream) {
+  return svo_cast_host_rows(sc, rays, n, 0, hits, stream);
 }
 
 svo_status svo_set_host_transfer(int32_t mode) {

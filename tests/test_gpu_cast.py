@@ -271,3 +271,54 @@ def test_batched_multi_scene_matches_single_scene_casts(oracle_mod):
             n = len(exp["status"])
             g = {k: v.cpu().numpy()[:n] for k, v in out.items()}
             assert_same_hits(g, exp, counters=True, label="batch item %d cfg %d/%d" % (j, cfg.block, cfg.rays_per_chunk))
+
+
+def test_row_layout_casts_equal_plain_casts(oracle_mod):
+    # svo_cast_rows / svo_cast_host_rows / svo_cast_lod_rows hand warps 8 x 4 blocks of an image's rays;
+    # the hits (and counters) are those of the plain calls, for any row length, with partial blocks
+    # at the right edge, a last band of fewer than 4 rows and batches below the work-queue size
+    torch = pytest.importorskip("torch")
+    ops = svo.gen_scene(0, 128, 4, seed=91, spheres=6, octaves=2, base_freq=1.0 / 32, height_lo=4.0, height_hi=80.0)
+    o, p = both(oracle_mod, 128, 4, ops)
+    W, H = 250, 163  # 40,750 rays: above the work-queue threshold
+    origins, dirs = svo.gen_camera_rays([200.0, 150.0, 220.0], [64.0, 40.0, 64.0], 60.0, W, H)
+    dev = torch.device("cuda:0")
+    s = torch.cuda.current_stream().cuda_stream
+
+    def device_cast(n, row, lod=None):
+        cols = {k: torch.from_numpy(np.ascontiguousarray(a[:n, i])).to(dev)
+                for a, names in ((origins, ("ox", "oy", "oz")), (dirs, ("dx", "dy", "dz"))) for i, k in enumerate(names)}
+        out = {k: torch.zeros(n, dtype=getattr(torch, np.dtype(t).name), device=dev) for k, t in svo.HIT_FIELDS.items()}
+        rp, hp = {k: v.data_ptr() for k, v in cols.items()}, {k: v.data_ptr() for k, v in out.items()}
+        if lod is None:
+            p.cast(rp, hp, n, s, row_length=row)
+        else:
+            p.cast_lod(rp, hp, n, lod, s, row_length=row)
+        torch.cuda.synchronize()
+        return {k: v.cpu().numpy() for k, v in out.items()}
+
+    def same(a, b, label):
+        for k in a:
+            assert np.array_equal(a[k], b[k], equal_nan=a[k].dtype.kind == "f"), (label, k)
+
+    n = len(origins)
+    plain = device_cast(n, 0)
+    assert_same_hits(plain, o.cast(origins, dirs, threads=8), counters=True, label="plain")
+    for row in (W, 8, 7, 13, 64, 1000, 5000, 1 << 20):
+        same(device_cast(n, row), plain, "rows %d" % row)
+    for m in (n - 37, 4 * W * 9 + 5, 20000):  # partial last band; below the work-queue size
+        same(device_cast(m, W), {k: v[:m] for k, v in plain.items()}, "rows %d, n %d" % (W, m))
+    # host buffers: in place (Grace) and staged in chunks of whole bands
+    for mode in (0, 1):
+        assert svo.lib().svo_set_host_transfer(mode) == 0
+        try:
+            same(p.cast_host(origins, dirs, row_length=W), plain, "host rows, transfer mode %d" % mode)
+        finally:
+            svo.lib().svo_set_host_transfer(0)
+    # the LOD cast with MIP maps
+    o.mip_switch(True)
+    p.switch_albedo_mip_maps(True)
+    p.sync()
+    lod_plain = device_cast(n, 0, lod=8.0)
+    same(device_cast(n, W, lod=8.0), lod_plain, "lod rows")
+    assert_same_hits(lod_plain, o.cast(origins, dirs, threads=8, viewing_distance=8.0), counters=True, label="lod")
