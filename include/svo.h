@@ -213,7 +213,8 @@ svo_status svo_cast_lod(svo_scene* scene, const svo_rays* rays, uint64_t n, cons
 svo_status svo_cast_host(svo_scene* scene, const svo_rays* rays, uint64_t n, const svo_hits* hits, void* stream);
 /* The three casts above for rays laid out as rows of row_length rays (a camera image in raster
  * order, or several images one after the other): the work queue hands each warp 8 neighbouring rays
- * of 4 neighbouring rows instead of 32 rays of one row, so its rays stay in step longer.  Hits are
+ * of 4 neighbouring rows instead of 32 rays of one row, so its rays stay in step longer (16 rays of
+ * 2 rows where svo_cast_host_rows reads the host's arrays in place).  Hits are
  * identical to the plain calls' (rays are independent); row_length 0, or a batch of fewer than 4
  * rows, casts in plain order.  No counterpart in the reference, whose renderer casts one pixel at a
  * time (examples/cpu_render.rs:104-138). */
@@ -254,6 +255,9 @@ typedef struct {
   svo_rays rays; /* device pointers */
   uint64_t n;
   svo_hits hits; /* device pointers */
+  uint32_t row_length; /* rays laid out as rows of this many rays (a camera image): cast in 8 x 4 ray
+                          blocks like svo_cast_rows; 0 = plain order */
+  uint32_t reserved;   /* 0 */
 } svo_batch_item;
 
 typedef struct {

@@ -320,14 +320,16 @@ class BatchWorkspace:
             self._h = None
 
     def cast(self, items, cfg=None, stream=0):
-        """items: list of (Octree, rays dict, n, hits dict) with device pointers."""
+        """items: list of (Octree, rays dict, n, hits dict[, row_length]) with device pointers."""
         from ._lib import BatchItem
         arr = (BatchItem * len(items))()
-        for i, (scene, rays, n, hits) in enumerate(items):
+        for i, item in enumerate(items):
+            scene, rays, n, hits = item[:4]
             arr[i].scene = scene.handle
             arr[i].rays = Rays(*[_vp(rays[k]) for k in ("ox", "oy", "oz", "dx", "dy", "dz")])
             arr[i].n = n
             arr[i].hits = Hits(**{k: _vp(hits.get(k, 0) or 0) for k in HIT_FIELDS})
+            arr[i].row_length = item[4] if len(item) > 4 else 0
         c = cfg if cfg is not None else LaunchConfig()
         check(lib().svo_cast_batched(self._h, arr, len(items), ctypes.byref(c), _vp(stream)))
 

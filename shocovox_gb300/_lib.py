@@ -79,7 +79,8 @@ class ServerStats(ctypes.Structure):
 
 
 class BatchItem(ctypes.Structure):
-    _fields_ = [("scene", ctypes.c_void_p), ("rays", Rays), ("n", ctypes.c_uint64), ("hits", Hits)]
+    _fields_ = [("scene", ctypes.c_void_p), ("rays", Rays), ("n", ctypes.c_uint64), ("hits", Hits),
+                ("row_length", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 # name -> (restype, argtypes); every symbol of include/svo.h is listed here

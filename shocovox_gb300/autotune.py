@@ -35,9 +35,9 @@ def _store(cache):
 
 def signature(items):
     """Workload class: item count and total rays (log2-bucketed), octree sizes and brick dims present."""
-    total = sum(n for _, _, n, _ in items)
-    sizes = sorted({s.size for s, _, _, _ in items})
-    dims = sorted({s.brick_dim for s, _, _, _ in items})
+    total = sum(it[2] for it in items)
+    sizes = sorted({it[0].size for it in items})
+    dims = sorted({it[0].brick_dim for it in items})
     return "items%d_rays2^%d_sizes%s_dims%s" % (len(items), max(total, 1).bit_length(), sizes, dims)
 
 

@@ -1,14 +1,15 @@
 // svo_batch.cu -- batched multi-scene cast: one persistent launch over many
 // (scene, ray batch) items.
 //
-// Work distribution: the rays of all items form one global index space
-// (item prefix sums).  Each warp repeatedly claims `rays_per_chunk`
-// consecutive indices from a device work counter with one atomicAdd, maps
-// every lane's index to its item by binary search over the prefix sums held
-// in shared memory, and casts with the shared per-ray restatement of
-// Octree::get_by_ray (svo_cast.cuh).  Items of different octree sizes and
-// brick dimensions mix freely; a ray's result does not depend on which warp
-// or launch casts it.
+// Work distribution: the claims of all items form one global index space
+// (item prefix sums; an item spans 32 indices per claim of its ClaimOrder, so
+// an item of camera rays with a row length is cast in 8 x 4 ray blocks).  Each
+// warp repeatedly claims `rays_per_chunk` consecutive indices from a device
+// work counter with one atomicAdd, maps every lane's index to its item by
+// binary search over the prefix sums held in shared memory, and casts with the
+// shared per-ray restatement of Octree::get_by_ray (svo_cast.cuh).  Items of
+// different octree sizes and brick dimensions mix freely; a ray's result does
+// not depend on which warp or launch casts it.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -25,9 +26,21 @@ struct BatchItemDev {
   SceneView scene;
   RaysView rays;
   HitsView hits;
-  uint64_t begin;  // first global ray index of the item
+  ClaimOrder order;  // the item's rays by claim and lane
+  uint64_t begin;    // first global index of the item (a multiple of 32)
   uint64_t n;
 };
+
+// fills the device form of one item at global index `begin`; returns the indices it spans
+uint64_t item_dev(const svo_batch_item& it, uint64_t begin, BatchItemDev& d) {
+  d.scene = scene_view(it.scene);
+  d.rays = RaysView{it.rays.ox, it.rays.oy, it.rays.oz, it.rays.dx, it.rays.dy, it.rays.dz};
+  d.hits = hits_view_of(it.hits);
+  d.order = claim_order(it.n, it.row_length);
+  d.begin = begin;
+  d.n = it.n;
+  return 32 * d.order.claims;
+}
 
 constexpr uint32_t kMaxSharedItems = 1024;  // prefix sums staged in shared memory
 
@@ -65,8 +78,9 @@ __global__ void __launch_bounds__(kBatchMaxBlock, 7)
           hi = mid - 1;
       }
       const BatchItemDev& it = items[lo];
-      const uint64_t i = g - it.begin;
-      if (i >= it.n) continue;  // an empty item shares its begin with the next one
+      const uint64_t x = g - it.begin;  // an empty item shares its begin with the next one
+      const uint64_t i = x < 32 * it.order.claims ? claimed_ray(it.order, x >> 5, (uint32_t)(x & 31u), it.n) : it.n;
+      if (i >= it.n) continue;
       const RaysView& r = it.rays;
       HitRecord h;
       cast_one<kCount>(it.scene, L, __ldg(r.ox + i), __ldg(r.oy + i), __ldg(r.oz + i), __ldg(r.dx + i),
@@ -155,13 +169,7 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
     if (!it.scene->dev.valid) return fail(SVO_ERR_NOT_UPLOADED, "svo_cast_batched: scene not uploaded");
     if (it.n && (!it.rays.ox || !it.rays.oy || !it.rays.oz || !it.rays.dx || !it.rays.dy || !it.rays.dz))
       return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: NULL ray array");
-    BatchItemDev& d = ws->h_items[i];
-    d.scene = scene_view(it.scene);
-    d.rays = RaysView{it.rays.ox, it.rays.oy, it.rays.oz, it.rays.dx, it.rays.dy, it.rays.dz};
-    d.hits = hits_view_of(it.hits);
-    d.begin = total;
-    d.n = it.n;
-    total += it.n;
+    total += item_dev(it, total, ws->h_items[i]);
     count |= counts_requested(it.hits);
   }
   if (total == 0) return SVO_OK;
@@ -259,13 +267,7 @@ svo_status svo_cast_batched_noalloc(const svo_batch_item* items, uint32_t n_item
     if (!it.scene->dev.valid) return fail(SVO_ERR_NOT_UPLOADED, "svo_cast_batched_noalloc: scene not uploaded");
     if (it.n && (!it.rays.ox || !it.rays.oy || !it.rays.oz || !it.rays.dx || !it.rays.dy || !it.rays.dz))
       return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: NULL ray array");
-    BatchItemDev& d = table[i];
-    d.scene = scene_view(it.scene);
-    d.rays = RaysView{it.rays.ox, it.rays.oy, it.rays.oz, it.rays.dx, it.rays.dy, it.rays.dz};
-    d.hits = hits_view_of(it.hits);
-    d.begin = total;
-    d.n = it.n;
-    total += it.n;
+    total += item_dev(it, total, table[i]);
     count |= counts_requested(it.hits);
   }
   if (total == 0) return SVO_OK;

@@ -30,6 +30,46 @@ constexpr uint32_t kOob = 8;
 constexpr uint32_t kWorkCap = 1u << 22;  // traversal steps per ray; the reference loops forever past it
 constexpr float kTol = 0.00001f;         // FLOAT_ERROR_TOLERANCE (src/spatial/raytracing/mod.rs:5)
 
+// ------------------------------------------------------------------ work claims
+// Which rays a warp's claim covers.  Rays laid out as rows of `row` rays (a camera image, or
+// several stacked) are claimed as blocks of 32 neighbouring rays, 2^shift wide and 32 / 2^shift
+// rows high, whose traversals stay in step far longer than 32 rays of one row; the rays past the
+// last full band of rows, and every ray of a batch without a row layout, are claimed 32
+// consecutive rays at a time.  Any order gives the same hits: rays are independent.
+struct ClaimOrder {
+  uint64_t row = 0;       // rays per row; 0: no row layout
+  uint64_t per_band = 0;  // blocks per band of rows
+  uint64_t blocks = 0;    // claims that are blocks
+  uint64_t tail = 0;      // first ray claimed 32 consecutive rays at a time
+  uint64_t claims = 0;    // claims in all
+  uint32_t shift = 3;     // log2 of the block width (3: 8 x 4, 4: 16 x 2)
+};
+
+inline ClaimOrder claim_order(uint64_t n, uint64_t row, uint32_t shift = 3) {
+  ClaimOrder o;
+  o.shift = shift;
+  const uint64_t width = 1ull << shift, band = (32ull >> shift) * row;
+  if (row >= width && n >= band) {
+    o.row = row;
+    o.per_band = (row + width - 1) / width;
+    o.blocks = (n / band) * o.per_band;
+    o.tail = (n / band) * band;
+  }
+  o.claims = o.blocks + (n - o.tail + 31) / 32;
+  return o;
+}
+
+// the ray of `lane` in claim c, or n when the lane has none
+__device__ __forceinline__ uint64_t claimed_ray(const ClaimOrder& o, uint64_t c, uint32_t lane, uint64_t n) {
+  if (c < o.blocks) {
+    const uint64_t band = c / o.per_band;
+    const uint64_t col = ((c - band * o.per_band) << o.shift) + (lane & ((1u << o.shift) - 1u));
+    return col < o.row ? ((band << (5 - o.shift)) + (lane >> o.shift)) * o.row + col : n;
+  }
+  const uint64_t i = o.tail + (c - o.blocks) * 32 + lane;
+  return i < n ? i : n;
+}
+
 // ------------------------------------------------------------------ Rust f32 semantics
 __device__ __forceinline__ float rmin(float a, float b) { return isnan(a) ? b : (isnan(b) ? a : (b < a ? b : a)); }
 __device__ __forceinline__ float rmax(float a, float b) { return isnan(a) ? b : (isnan(b) ? a : (b > a ? b : a)); }

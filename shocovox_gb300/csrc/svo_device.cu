@@ -31,41 +31,6 @@ __global__ void __launch_bounds__(128, 7) cast_kernel(SceneView s, RaysView rays
   if (kCount) write_counters(out, i, h);
 }
 
-// Which rays a warp's claim covers.  Rays laid out as rows of `row` rays (a camera image, or
-// several stacked) are claimed as blocks of 8 neighbouring rays in 4 neighbouring rows, whose
-// traversals stay in step far longer than 32 rays of one row; the rays past the last full band
-// of 4 rows, and every ray of a batch without a row layout, are claimed 32 consecutive rays at a
-// time.  Any order gives the same hits: rays are independent.
-struct ClaimOrder {
-  uint64_t row = 0;       // rays per row; 0: no row layout
-  uint64_t per_band = 0;  // 8-ray blocks per band of 4 rows
-  uint64_t blocks = 0;    // claims that are blocks
-  uint64_t tail = 0;      // first ray claimed 32 consecutive rays at a time
-  uint64_t claims = 0;    // claims in all
-};
-
-ClaimOrder claim_order(uint64_t n, uint64_t row) {
-  ClaimOrder o;
-  if (row >= 8 && n >= 4 * row) {
-    o.row = row;
-    o.per_band = (row + 7) / 8;
-    o.blocks = (n / (4 * row)) * o.per_band;
-    o.tail = (n / (4 * row)) * 4 * row;
-  }
-  o.claims = o.blocks + (n - o.tail + 31) / 32;
-  return o;
-}
-
-// the ray of `lane` in claim c, or n when the lane has none
-__device__ __forceinline__ uint64_t claimed_ray(const ClaimOrder& o, uint64_t c, uint32_t lane, uint64_t n) {
-  if (c < o.blocks) {
-    const uint64_t band = c / o.per_band, col = (c - band * o.per_band) * 8 + (lane & 7u);
-    return col < o.row ? (band * 4 + (lane >> 3)) * o.row + col : n;
-  }
-  const uint64_t i = o.tail + (c - o.blocks) * 32 + lane;
-  return i < n ? i : n;
-}
-
 // Queued cast: a persistent grid whose warps claim 32 rays at a time from a work counter.  The
 // cost of a ray varies by orders of magnitude (a sky ray leaves after a few node visits, a
 // grazing ray walks a whole cave), and a warp that finishes early takes more work instead of
@@ -356,8 +321,11 @@ svo_status incremental_sync(svo_scene* sc, cudaStream_t st) {
 }
 
 
+// `in_place`: rays and hits are host memory the device reads and writes through the CPU's page
+// tables; the claims are then 16 x 2 blocks (two 64-byte pieces of each array per warp instead of
+// four 32-byte ones), which the host link serves faster than 8 x 4 blocks.
 svo_status launch_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_hits* hits, cudaStream_t st,
-                       uint64_t row = 0) {
+                       uint64_t row = 0, bool in_place = false) {
   if (n == 0) return SVO_OK;
   const SceneView v = scene_view(sc);
   RaysView rv{rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz};
@@ -371,7 +339,7 @@ svo_status launch_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const sv
       const int per_sm = std::max(1, count ? q->blocks_per_sm_count : q->blocks_per_sm);
       const uint64_t grid = std::min<uint64_t>((uint64_t)q->sm_count * per_sm, (n + block - 1) / block);
       SVO_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st));
-      const ClaimOrder order = claim_order(n, row);
+      const ClaimOrder order = claim_order(n, row, in_place ? 4 : 3);
       if (count)
         queue_kernel<true><<<(unsigned)grid, block, 0, st>>>(v, rv, hv, n, order, ctr);
       else
@@ -625,7 +593,7 @@ svo_status svo_cast_host_rows(svo_scene* sc, const svo_rays* rays, uint64_t n, u
       return fail(SVO_ERR_ARGUMENT, "svo_cast_host: this device cannot access host memory directly");
   }
   if (!direct) return cast_host_pipelined(sc, rays, n, hits, st, row_length);
-  const svo_status rc = launch_cast(sc, rays, n, hits, st, row_length);
+  const svo_status rc = launch_cast(sc, rays, n, hits, st, row_length, true);
   if (rc != SVO_OK) return rc;
   SVO_CUDA_TRY(cudaStreamSynchronize(st));
   return SVO_OK;

@@ -203,6 +203,7 @@ svo_status launch(svo_server* sv, LaunchSlot& ls, size_t n_scenes, LaunchCounts&
     it.scene = sv->scenes[q->r.scene_id].scene;
     it.rays = svo_rays{r[0], r[1], r[2], r[3], r[4], r[5]};
     it.n = q->n;
+    it.row_length = q->r.width;  // camera rays in raster order
     void* const* hf = reinterpret_cast<void* const*>(&q->r.hits);
     void** df = reinterpret_cast<void**>(&it.hits);
     for (int fi = 0; fi < kHitFields; ++fi)

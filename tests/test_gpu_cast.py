@@ -243,8 +243,10 @@ def test_batched_multi_scene_matches_single_scene_casts(oracle_mod):
     dev = torch.device("cuda:0")
     rng = np.random.default_rng(9)
     scenes, items, expected, keep = [], [], [], []
-    for j, (kind, size, dim, nrays) in enumerate([(3, 64, 2, 3000), (0, 128, 4, 5000), (3, 32, 8, 0),
-                                                  (1, 64, 8, 2000), (2, 128, 4, 4000), (3, 64, 1, 1500)]):
+    # the row lengths lay the items out as images (8 x 4 ray blocks, partial blocks and bands included)
+    for j, (kind, size, dim, nrays, row) in enumerate([(3, 64, 2, 3000, 50), (0, 128, 4, 5000, 0), (3, 32, 8, 0, 8),
+                                                       (1, 64, 8, 2000, 33), (2, 128, 4, 4000, 7),
+                                                       (3, 64, 1, 1500, 1500)]):
         ops = svo.gen_scene(kind, size, dim, seed=200 + j, occupancy=0.1, spheres=2, octaves=2, base_freq=1.0 / 16,
                             height_lo=2.0, height_hi=size * 0.3)
         o, p = both(oracle_mod, size, dim, ops)
@@ -254,7 +256,8 @@ def test_batched_multi_scene_matches_single_scene_casts(oracle_mod):
                 for i, k in enumerate(names)}
         out = {k: torch.zeros(max(nrays, 1), dtype=getattr(torch, np.dtype(t).name), device=dev)
                for k, t in svo.HIT_FIELDS.items()}
-        items.append((p, {k: v.data_ptr() for k, v in cols.items()}, nrays, {k: v.data_ptr() for k, v in out.items()}))
+        items.append((p, {k: v.data_ptr() for k, v in cols.items()}, nrays, {k: v.data_ptr() for k, v in out.items()},
+                      row))
         expected.append(o.cast(origins, dirs) if nrays else None)
         scenes.append(p)
         keep.append((cols, out))
