@@ -591,8 +591,8 @@ __device__ __forceinline__ uint32_t probe_brick_fast(const SceneView& s, FastRay
   uint32_t move = 0;
   for (;;) {
     if ((unsigned)cx >= (unsigned)D || (unsigned)cy >= (unsigned)D || (unsigned)cz >= (unsigned)D) return 0;
+    // flat == cx + cy D + cz D^2 (moved with the index), inside the brick like the index
     flat += ((move & 1u) ? fdx : 0) + ((move & 4u) ? fdy : 0) + ((move & 2u) ? fdz : 0);
-    if ((unsigned)flat >= (unsigned)D3) return 3;
     if (kCount) h.vreads++;
     if (++work > kWorkCap) return 2;
     if ((__ldg(bits + (flat >> 5)) >> (flat & 31)) & 1u) {
