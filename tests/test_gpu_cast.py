@@ -312,10 +312,15 @@ def test_row_layout_casts_equal_plain_casts(oracle_mod):
     for m in (n - 37, 4 * W * 9 + 5, 20000):  # partial last band; below the work-queue size
         same(device_cast(m, W), {k: v[:m] for k, v in plain.items()}, "rows %d, n %d" % (W, m))
     # host buffers: in place (Grace) and staged in chunks of whole bands
+    # (with and without counters: the instrumented cast is a kernel of its own)
+    no_counters = [k for k in svo.HIT_FIELDS if k not in COUNTERS + ["run_visits"]]
     for mode in (0, 1):
         assert svo.lib().svo_set_host_transfer(mode) == 0
         try:
             same(p.cast_host(origins, dirs, row_length=W), plain, "host rows, transfer mode %d" % mode)
+            for m, row in ((n, W), (n - 37, W), (n, 40), (n, 31), (4 * W * 9 + 5, W)):
+                got = p.cast_host(origins[:m], dirs[:m], fields=no_counters, row_length=row)
+                same(got, {k: plain[k][:m] for k in no_counters}, "host rows %d, n %d, mode %d" % (row, m, mode))
         finally:
             svo.lib().svo_set_host_transfer(0)
     # the LOD cast with MIP maps
