@@ -633,29 +633,55 @@ __device__ __forceinline__ uint32_t probe_mip(const SceneView& s, FastRay& r, ui
 
 // kLod: get_by_ray_at_lod with MIP maps (s.mips): the MIP reads of the literal form, and restart
 // runs taken in closed form only where lod_runs_clear proves that none of their visits reads a MIP.
-template <bool kCount, bool kLod = false>
-__device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox, float oy, float oz, float dx,
-                              float dy, float dz, HitRecord& h, float viewing_distance = 0.0f) {
+// The record of a ray that hits nothing.
+__device__ __forceinline__ void miss_record(HitRecord& h) {
   h.status = 0;
   h.octant = 0;
   h.node = 0;
   h.voxel = 0xFFFFFFFFu;
   h.pix = 0;
   h.px = h.py = h.pz = h.nx = h.ny = h.nz = 0.0f;
-  if (kCount) h.visits = h.creads = h.vreads = h.runs = 0;
+  h.visits = h.creads = h.vreads = h.runs = 0;
+}
 
+// The fast form's way into the octree (get_by_ray's root intersection, :330-348): false when the ray
+// misses the root box; else the point where it enters (its origin when inside) and that point's
+// octant of the root.
+__device__ __forceinline__ bool fast_entry(const SceneView& s, float ox, float oy, float oz, float dx, float dy,
+                                           float dz, float& px, float& py, float& pz, uint32_t& target) {
+  const float S = s.size;
   // A ray whose origin lies outside the octree on some axis and that moves further away on it has
   // both of that axis' slab distances negative, so tmax < 0 and the slab test below rejects it.
   // The quotients are strictly negative when the origin is finite, at least 2^-100 below 0 (or
   // above S) and the direction component at most 2^20 in size: no quotient rounds to -0.
   {
-    const float S = s.size, lo = -0x1p-100f, big = 0x1p20f;
+    const float lo = -0x1p-100f, big = 0x1p20f;
     const bool fin = isfinite(ox) && isfinite(oy) && isfinite(oz) && fabsf(dx) <= big && fabsf(dy) <= big &&
                      fabsf(dz) <= big;
     if (fin && ((ox < lo && dx < 0.0f) || (ox > S && dx > 0.0f) || (oy < lo && dy < 0.0f) || (oy > S && dy > 0.0f) ||
                 (oz < lo && dz < 0.0f) || (oz > S && dz > 0.0f)))
-      return;
+      return false;
   }
+  const float t1 = (0.0f - ox) / dx, t2 = ((0.0f + S) - ox) / dx;
+  const float t3 = (0.0f - oy) / dy, t4 = ((0.0f + S) - oy) / dy;
+  const float t5 = (0.0f - oz) / dz, t6 = ((0.0f + S) - oz) / dz;
+  const float tmin = rmax(rmax(rmin(t1, t2), rmin(t3, t4)), rmin(t5, t6));
+  const float tmax = rmin(rmin(rmax(t1, t2), rmax(t3, t4)), rmax(t5, t6));
+  if (tmax < 0.0f || tmin > tmax) return false;
+  const float t = tmin < 0.0f ? 0.0f : tmin;
+  px = ox + dx * t;
+  py = oy + dy * t;
+  pz = oz + dz * t;
+  target = hash_region(px - 0.0f, py - 0.0f, pz - 0.0f, S * 0.5f);
+  return true;
+}
+
+// The fast form's traversal of a ray that entered the root at (px, py, pz), in its octant `target`.
+template <bool kCount, bool kLod = false>
+__device__ void cast_ray_fast_from(const SceneView& s, const SharedLuts& L, float ox, float oy, float oz, float dx,
+                                   float dy, float dz, float px, float py, float pz, uint32_t target, HitRecord& h,
+                                   float viewing_distance = 0.0f) {
+  miss_record(h);
   FastRay r;
   r.dx = dx;
   r.dy = dy;
@@ -667,20 +693,9 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
   const uint64_t* rtn = L.ray_to_node + dir;
   const float S = s.size;
   Bounds cb{0.0f, 0.0f, 0.0f, S, s.inv_size};
-  uint32_t target;
-  {
-    const float t1 = (0.0f - ox) / dx, t2 = ((0.0f + S) - ox) / dx;
-    const float t3 = (0.0f - oy) / dy, t4 = ((0.0f + S) - oy) / dy;
-    const float t5 = (0.0f - oz) / dz, t6 = ((0.0f + S) - oz) / dz;
-    const float tmin = rmax(rmax(rmin(t1, t2), rmin(t3, t4)), rmin(t5, t6));
-    const float tmax = rmin(rmin(rmax(t1, t2), rmax(t3, t4)), rmax(t5, t6));
-    if (tmax < 0.0f || tmin > tmax) return;
-    const float t = tmin < 0.0f ? 0.0f : tmin;
-    r.px = ox + dx * t;
-    r.py = oy + dy * t;
-    r.pz = oz + dz * t;
-    target = hash_region(r.px - 0.0f, r.py - 0.0f, r.pz - 0.0f, S * 0.5f);
-  }
+  r.px = px;
+  r.py = py;
+  r.pz = pz;
   {  // get_dda_scale_factors (:99-112), a function of the direction only, so formed after the
      // root's slab test has let the ray in; powf(q, 2.) == q * q
     const float a = dz / dx, b = dy / dx, c = dx / dy, d = dz / dy, e = dx / dz, f = dy / dz;
@@ -886,6 +901,18 @@ __device__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox,
   }
 }
 
+template <bool kCount, bool kLod = false>
+__device__ __forceinline__ void cast_ray_fast(const SceneView& s, const SharedLuts& L, float ox, float oy, float oz,
+                                              float dx, float dy, float dz, HitRecord& h,
+                                              float viewing_distance = 0.0f) {
+  float px, py, pz;
+  uint32_t target;
+  if (fast_entry(s, ox, oy, oz, dx, dy, dz, px, py, pz, target))
+    cast_ray_fast_from<kCount, kLod>(s, L, ox, oy, oz, dx, dy, dz, px, py, pz, target, h, viewing_distance);
+  else
+    miss_record(h);
+}
+
 // Rays whose direction holds a NaN take the literal form, out of line so that
 // it does not add to the fast path's register allocation.
 template <bool kCount>
@@ -899,6 +926,20 @@ template <bool kCount>
 __device__ __noinline__ void cast_ray_literal_lod(const SceneView& s, const SharedLuts& L, float ox, float oy, float oz,
                                                   float dx, float dy, float dz, HitRecord& h, float viewing_distance) {
   cast_ray<kCount, false, true>(s, L, ox, oy, oz, dx, dy, dz, h, viewing_distance);
+}
+
+// cast_one for a ray whose way in is known: `fast` with its fast_entry (px, py, pz, target), else the
+// literal form (a NaN in the direction, or literal mode).
+template <bool kCount, bool kLod = false>
+__device__ __forceinline__ void cast_entered(const SceneView& s, const SharedLuts& L, float ox, float oy, float oz,
+                                             float dx, float dy, float dz, bool fast, float px, float py, float pz,
+                                             uint32_t target, HitRecord& h, float viewing_distance = 0.0f) {
+  if (fast)
+    cast_ray_fast_from<kCount, kLod>(s, L, ox, oy, oz, dx, dy, dz, px, py, pz, target, h, viewing_distance);
+  else if (kLod)
+    cast_ray_literal_lod<kCount>(s, L, ox, oy, oz, dx, dy, dz, h, viewing_distance);
+  else
+    cast_ray_literal<kCount>(s, L, ox, oy, oz, dx, dy, dz, h);
 }
 
 // One ray: the exact fast form when the direction holds no NaN, the literal form otherwise; kLod

@@ -35,24 +35,108 @@ __global__ void __launch_bounds__(128, 7) cast_kernel(SceneView s, RaysView rays
 // cost of a ray varies by orders of magnitude (a sky ray leaves after a few node visits, a
 // grazing ray walks a whole cave), and a warp that finishes early takes more work instead of
 // idling until its block's slowest warp is done.  The counter (claims taken) starts at 0.
+//
+// Rays that miss the octree's root box get their miss written at once.  A claim whose rays all
+// enter is cast as it is; the entering rays of other claims wait in the warp's slice of shared
+// memory, with the point where they enter, until 32 of them fill the warp, so that rays from
+// outside the octree (most of them missing it) do not leave most lanes idle.
+struct WaitingRays {
+  float o[3][64], d[3][64], p[3][64];
+  uint32_t target[64];  // octant of the entry point; bit 31: fast form
+  unsigned long long i[64];
+};
+
 template <bool kCount, bool kLod = false>
 __global__ void __launch_bounds__(128, 7)
     queue_kernel(SceneView s, RaysView rays, HitsView out, uint64_t n, ClaimOrder order,
                  unsigned long long* __restrict__ counter, float viewing_distance = 0.0f) {
   __shared__ SharedLuts L;
+  __shared__ WaitingRays waiting[4];
   fill_shared_luts(L);
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31u;
+  WaitingRays& w = waiting[threadIdx.x >> 5];
+  uint32_t count = 0;  // rays waiting (the same in every lane)
+  bool more = true;    // claims left
   for (;;) {
-    unsigned long long c = 0;
-    if (lane == 0) c = atomicAdd(counter, 1ull);
-    c = __shfl_sync(0xFFFFFFFFu, c, 0);
-    if (c >= order.claims) break;
-    const uint64_t i = claimed_ray(order, c, lane, n);
-    if (i >= n) continue;
+    bool have = false, fast = false;
+    uint64_t i = 0;
+    float ox = 0.0f, oy = 0.0f, oz = 0.0f, dx = 0.0f, dy = 0.0f, dz = 0.0f, px = 0.0f, py = 0.0f, pz = 0.0f;
+    uint32_t target = 0;
+    while (more && count < 32) {
+      unsigned long long c = 0;
+      if (lane == 0) c = atomicAdd(counter, 1ull);
+      c = __shfl_sync(0xFFFFFFFFu, c, 0);
+      if (c >= order.claims) {
+        more = false;
+        break;
+      }
+      const uint64_t j = claimed_ray(order, c, lane, n);
+      bool enters = false;
+      if (j < n) {
+        ox = __ldg(rays.ox + j);
+        oy = __ldg(rays.oy + j);
+        oz = __ldg(rays.oz + j);
+        dx = __ldg(rays.dx + j);
+        dy = __ldg(rays.dy + j);
+        dz = __ldg(rays.dz + j);
+        fast = !s.literal && !isnan(dx) && !isnan(dy) && !isnan(dz);
+        enters = !fast || fast_entry(s, ox, oy, oz, dx, dy, dz, px, py, pz, target);
+        if (!enters) {
+          HitRecord h;
+          miss_record(h);
+          write_hit(s, out, j, h);
+          if (kCount) write_counters(out, j, h);
+        }
+      }
+      const unsigned m = __ballot_sync(0xFFFFFFFFu, enters);
+      if (m == 0xFFFFFFFFu && count == 0) {  // a full claim: cast in place
+        have = true;
+        i = j;
+        break;
+      }
+      if (enters) {
+        const uint32_t k = count + __popc(m & ((1u << lane) - 1u));
+        w.o[0][k] = ox;
+        w.o[1][k] = oy;
+        w.o[2][k] = oz;
+        w.d[0][k] = dx;
+        w.d[1][k] = dy;
+        w.d[2][k] = dz;
+        w.p[0][k] = px;
+        w.p[1][k] = py;
+        w.p[2][k] = pz;
+        w.target[k] = target | (fast ? 0x80000000u : 0u);
+        w.i[k] = j;
+      }
+      count += __popc(m);
+      __syncwarp();
+    }
+    if (!have) {
+      if (count == 0) break;  // no claims left and nothing waiting
+      const uint32_t take = count < 32 ? count : 32;
+      if (lane < take) {
+        const uint32_t k = count - take + lane;
+        ox = w.o[0][k];
+        oy = w.o[1][k];
+        oz = w.o[2][k];
+        dx = w.d[0][k];
+        dy = w.d[1][k];
+        dz = w.d[2][k];
+        px = w.p[0][k];
+        py = w.p[1][k];
+        pz = w.p[2][k];
+        target = w.target[k] & 0x7FFFFFFFu;
+        fast = (w.target[k] >> 31) != 0u;
+        i = w.i[k];
+        have = true;
+      }
+      count -= take;
+      __syncwarp();
+    }
+    if (!have) continue;
     HitRecord h;
-    cast_one<kCount, kLod>(s, L, __ldg(rays.ox + i), __ldg(rays.oy + i), __ldg(rays.oz + i), __ldg(rays.dx + i),
-                     __ldg(rays.dy + i), __ldg(rays.dz + i), h, viewing_distance);
+    cast_entered<kCount, kLod>(s, L, ox, oy, oz, dx, dy, dz, fast, px, py, pz, target, h, viewing_distance);
     write_hit(s, out, i, h);
     if (kCount) write_counters(out, i, h);
   }

@@ -330,3 +330,38 @@ def test_row_layout_casts_equal_plain_casts(oracle_mod):
     lod_plain = device_cast(n, 0, lod=8.0)
     same(device_cast(n, W, lod=8.0), lod_plain, "lod rows")
     assert_same_hits(lod_plain, o.cast(origins, dirs, threads=8, viewing_distance=8.0), counters=True, label="lod")
+
+
+def test_work_queue_with_rays_missing_the_root(oracle_mod):
+    # batches above the work-queue size whose rays mostly miss the root box: the queue writes those
+    # misses at once and packs the entering rays into full warps (NaN directions and the literal
+    # mode included); every field and counter equals the oracle's
+    torch = pytest.importorskip("torch")
+    ops = svo.gen_scene(3, 64, 4, seed=31, occupancy=0.12, spheres=3, octaves=2, base_freq=1.0 / 16)
+    o, p = both(oracle_mod, 64, 4, ops)
+    rng = np.random.default_rng(77)
+    n = 50000
+    origins = rng.uniform(-200.0, 264.0, size=(n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3))
+    dirs = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    dirs[::997] = np.float32(np.nan)
+    origins[5000:5100] = np.float32(32.0)  # a run of rays from inside: whole claims that all enter
+    dev = torch.device("cuda:0")
+    cols = {k: torch.from_numpy(np.ascontiguousarray(a[:, i])).to(dev)
+            for a, names in ((origins, ("ox", "oy", "oz")), (dirs, ("dx", "dy", "dz"))) for i, k in enumerate(names)}
+    s = torch.cuda.current_stream().cuda_stream
+    want = o.cast(origins, dirs, threads=8)
+    assert 0.5 < (want["node_visits"] == 0).mean() < 0.99
+    for mode in (0, 1):
+        assert svo.lib().svo_set_cast_mode(mode) == 0
+        try:
+            for with_counters in (True, False):
+                out = {k: torch.zeros(n, dtype=getattr(torch, np.dtype(t).name), device=dev)
+                       for k, t in svo.HIT_FIELDS.items()
+                       if with_counters or k not in COUNTERS + ["run_visits"]}
+                p.cast({k: v.data_ptr() for k, v in cols.items()}, {k: v.data_ptr() for k, v in out.items()}, n, s)
+                torch.cuda.synchronize()
+                g = {k: v.cpu().numpy() for k, v in out.items()}
+                assert_same_hits(g, want, counters=with_counters, label="queue mode %d" % mode)
+        finally:
+            svo.lib().svo_set_cast_mode(0)
