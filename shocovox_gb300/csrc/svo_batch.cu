@@ -48,49 +48,142 @@ constexpr uint32_t kMaxSharedItems = 1024;  // prefix sums staged in shared memo
 // spilled bytes); the launch configuration is checked against the block limit.
 constexpr uint32_t kBatchMaxBlock = 128;
 
+// Rays that miss their octree's root box get their miss written at once; the entering rays of a
+// partly entering round of 32 indices wait in the warp's slice of shared memory (with the point where
+// they enter and their item) until 32 of them fill the warp.
+struct WaitingBatchRays {
+  float o[3][64], d[3][64], p[3][64];
+  uint32_t target[64];  // octant of the entry point; bit 31: fast form
+  uint32_t item[64];
+  unsigned long long i[64];
+};
+
 template <bool kCount>
 __global__ void __launch_bounds__(kBatchMaxBlock, 7)
     batched_kernel(const BatchItemDev* __restrict__ items, uint32_t n_items, uint64_t total,
                    unsigned long long* __restrict__ counter, uint32_t chunk) {
   __shared__ uint64_t s_begin[kMaxSharedItems];
   __shared__ SharedLuts L;
+  __shared__ WaitingBatchRays waiting[kBatchMaxBlock / 32];
   const uint32_t staged = n_items < kMaxSharedItems ? n_items : kMaxSharedItems;
   for (uint32_t i = threadIdx.x; i < staged; i += blockDim.x) s_begin[i] = items[i].begin;
   fill_shared_luts(L);
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31u;
+  WaitingBatchRays& w = waiting[threadIdx.x >> 5];
+  uint32_t count = 0;                 // rays waiting (the same in every lane)
+  bool more = true;                   // chunks left
+  unsigned long long base = 0;        // the warp's chunk
+  uint32_t next = chunk;              // offset of the next round of 32 indices in it
   for (;;) {
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(counter, (unsigned long long)chunk);
-    base = __shfl_sync(0xFFFFFFFFu, base, 0);
-    if (base >= total) break;
-    for (uint32_t k = lane; k < chunk; k += 32) {
-      const uint64_t g = base + k;
-      if (g >= total) break;
-      // largest item with begin <= g (items are sorted by begin)
-      uint32_t lo = 0, hi = n_items - 1;
-      while (lo < hi) {
-        const uint32_t mid = (lo + hi + 1) >> 1;
-        const uint64_t b = mid < kMaxSharedItems ? s_begin[mid] : items[mid].begin;
-        if (b <= g)
-          lo = mid;
-        else
-          hi = mid - 1;
+    bool have = false, fast = false;
+    uint64_t i = 0;
+    uint32_t item = 0, target = 0;
+    float ox = 0.0f, oy = 0.0f, oz = 0.0f, dx = 0.0f, dy = 0.0f, dz = 0.0f, px = 0.0f, py = 0.0f, pz = 0.0f;
+    while (count < 32) {
+      if (next >= chunk) {
+        if (!more) break;
+        if (lane == 0) base = atomicAdd(counter, (unsigned long long)chunk);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= total) {
+          more = false;
+          break;
+        }
+        next = 0;
       }
-      const BatchItemDev& it = items[lo];
-      const uint64_t x = g - it.begin;  // an empty item shares its begin with the next one
-      const uint64_t i = x < 32 * it.order.claims ? claimed_ray(it.order, x >> 5, (uint32_t)(x & 31u), it.n) : it.n;
-      if (i >= it.n) continue;
-      const RaysView& r = it.rays;
-      HitRecord h;
-      cast_one<kCount>(it.scene, L, __ldg(r.ox + i), __ldg(r.oy + i), __ldg(r.oz + i), __ldg(r.dx + i),
-                       __ldg(r.dy + i), __ldg(r.dz + i), h);
-      write_hit(it.scene, it.hits, i, h);
-      if (kCount) write_counters(it.hits, i, h);
+      const uint64_t g = base + next + lane;
+      const bool in_chunk = next + lane < chunk;
+      next += 32;
+      bool enters = false;
+      if (in_chunk && g < total) {
+        // largest item with begin <= g (items are sorted by begin)
+        uint32_t lo = 0, hi = n_items - 1;
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi + 1) >> 1;
+          const uint64_t b = mid < kMaxSharedItems ? s_begin[mid] : items[mid].begin;
+          if (b <= g)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+        const BatchItemDev& it = items[lo];
+        const uint64_t x = g - it.begin;  // an empty item shares its begin with the next one
+        const uint64_t j =
+            x < 32 * it.order.claims ? claimed_ray(it.order, x >> 5, (uint32_t)(x & 31u), it.n) : it.n;
+        if (j < it.n) {
+          const RaysView& r = it.rays;
+          ox = __ldg(r.ox + j);
+          oy = __ldg(r.oy + j);
+          oz = __ldg(r.oz + j);
+          dx = __ldg(r.dx + j);
+          dy = __ldg(r.dy + j);
+          dz = __ldg(r.dz + j);
+          fast = !it.scene.literal && !isnan(dx) && !isnan(dy) && !isnan(dz);
+          enters = !fast || fast_entry(it.scene, ox, oy, oz, dx, dy, dz, px, py, pz, target);
+          if (!enters) {
+            HitRecord h;
+            miss_record(h);
+            write_hit(it.scene, it.hits, j, h);
+            if (kCount) write_counters(it.hits, j, h);
+          }
+          i = j;
+          item = lo;
+        }
+      }
+      const unsigned m = __ballot_sync(0xFFFFFFFFu, enters);
+      if (m == 0xFFFFFFFFu && count == 0) {  // a full round: cast in place
+        have = true;
+        break;
+      }
+      if (enters) {
+        const uint32_t k = count + __popc(m & ((1u << lane) - 1u));
+        w.o[0][k] = ox;
+        w.o[1][k] = oy;
+        w.o[2][k] = oz;
+        w.d[0][k] = dx;
+        w.d[1][k] = dy;
+        w.d[2][k] = dz;
+        w.p[0][k] = px;
+        w.p[1][k] = py;
+        w.p[2][k] = pz;
+        w.target[k] = target | (fast ? 0x80000000u : 0u);
+        w.item[k] = item;
+        w.i[k] = i;
+      }
+      count += __popc(m);
+      __syncwarp();
     }
+    if (!have) {
+      if (count == 0) break;  // no chunks left and nothing waiting
+      const uint32_t take = count < 32 ? count : 32;
+      if (lane < take) {
+        const uint32_t k = count - take + lane;
+        ox = w.o[0][k];
+        oy = w.o[1][k];
+        oz = w.o[2][k];
+        dx = w.d[0][k];
+        dy = w.d[1][k];
+        dz = w.d[2][k];
+        px = w.p[0][k];
+        py = w.p[1][k];
+        pz = w.p[2][k];
+        target = w.target[k] & 0x7FFFFFFFu;
+        fast = (w.target[k] >> 31) != 0u;
+        item = w.item[k];
+        i = w.i[k];
+        have = true;
+      }
+      count -= take;
+      __syncwarp();
+    }
+    if (!have) continue;
+    const BatchItemDev& it = items[item];
+    HitRecord h;
+    cast_entered<kCount>(it.scene, L, ox, oy, oz, dx, dy, dz, fast, px, py, pz, target, h);
+    write_hit(it.scene, it.hits, i, h);
+    if (kCount) write_counters(it.hits, i, h);
   }
 }
-
 
 }  // namespace svo
 
