@@ -248,6 +248,12 @@ typedef struct {
  * not reset).  Allocates nothing; rays never touch memory. */
 svo_status svo_render_viewport(svo_scene* scene, const svo_viewport* viewport, uint32_t width_px, uint32_t height_px,
                                uint8_t* rgba, unsigned long long* unshaded, void* stream);
+/* n_views viewports of one scene, each W x H, frame k at rgba + k * W * H * 4: the same pixels as
+ * n_views svo_render_viewport calls, in one launch per 16 views (a launch's last tiles no longer
+ * leave the GPU idle once per frame).  Pixels whose ray misses the octree's root box are coloured
+ * at once; the rays that enter are packed into full warps. */
+svo_status svo_render_viewports(svo_scene* scene, const svo_viewport* viewports, uint32_t n_views, uint32_t width_px,
+                                uint32_t height_px, uint8_t* rgba, unsigned long long* unshaded, void* stream);
 
 /* ---- batched multi-scene cast (one persistent launch) ------------------ */
 typedef struct {

@@ -270,6 +270,13 @@ class Octree:
         check(lib().svo_render_viewport(self._h, ctypes.byref(viewport), width, height, _vp(rgba), _vp(unshaded),
                                         _vp(stream)))
 
+    def render_viewports(self, viewports, width, height, rgba, unshaded=0, stream=0):
+        """Several viewports in one launch: frame k at rgba + k * height * width * 4."""
+        from ._lib import Viewport
+        arr = (Viewport * len(viewports))(*viewports)
+        check(lib().svo_render_viewports(self._h, arr, len(viewports), width, height, _vp(rgba), _vp(unshaded),
+                                         _vp(stream)))
+
     def get_by_ray(self, origin, direction):
         """Octree::get_by_ray for one ray: None or ((kind, rgba, user), point, normal)."""
         r = self.cast_host([origin], [direction])

@@ -126,6 +126,7 @@ SIGNATURES = {
     "svo_cast_host_rows": (_I32, [_VP, _P(Rays), _U64, _U32, _P(Hits), _VP]),
     "svo_cast_lod_rows": (_I32, [_VP, _P(Rays), _U64, _U32, _P(Hits), ctypes.c_float, _VP]),
     "svo_render_viewport": (_I32, [_VP, _P(Viewport), _U32, _U32, _VP, _VP, _VP]),
+    "svo_render_viewports": (_I32, [_VP, _P(Viewport), _U32, _U32, _U32, _VP, _VP, _VP]),
     "svo_batch_workspace_create": (_I32, [_P(_VP)]),
     "svo_batch_workspace_destroy": (None, [_VP]),
     "svo_cast_batched": (_I32, [_VP, _P(BatchItem), _U32, _P(LaunchConfig), _VP]),

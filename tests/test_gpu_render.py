@@ -78,3 +78,33 @@ def test_render_rejects_bad_arguments():
         p.render_viewport(svo.orbit_viewport(0.0, 30.0), 8, 8, 0)  # NULL output
     with pytest.raises(SvoError):  # not uploaded
         p.render_viewport(svo.orbit_viewport(0.0, 30.0), 8, 8, 64)
+
+
+def test_several_viewports_in_one_launch_equal_single_renders(oracle_mod):
+    # svo_render_viewports: frame k of one launch is svo_render_viewport's image of view k, also past 16
+    # views (two launches) and with sky pixels (rays missing the root box) mixed in
+    ops = svo.gen_scene(0, 128, 4, seed=0x5EED0001, spheres=8, octaves=2, base_freq=1.0 / 32, height_lo=0.0,
+                        height_hi=96.0)
+    o, p = both(oracle_mod, 128, 4, ops)
+    vps = [aimed(0.37 * k, 160.0 + 7 * k, 64.0) for k in range(19)]
+    W, H = 72, 40
+    dev = torch.device("cuda", 0)
+    img = torch.zeros((len(vps), H, W, 4), dtype=torch.uint8, device=dev)
+    bad = torch.zeros(1, dtype=torch.int64, device=dev)
+    p.render_viewports(vps, W, H, img.data_ptr(), bad.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    got = img.cpu().numpy()
+    for k, vp in enumerate(vps):
+        single, _ = render_gpu(p, vp, W, H)
+        assert np.array_equal(got[k], single), k
+    want, _ = o.render_viewport(vp_dict(vps[3]), W, H, threads=8)
+    assert np.array_equal(got[3], want)
+    # a large frame (work queue), 3 views
+    W, H = 300, 200
+    img = torch.zeros((3, H, W, 4), dtype=torch.uint8, device=dev)
+    p.render_viewports(vps[:3], W, H, img.data_ptr(), bad.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    got = img.cpu().numpy()
+    for k in range(3):
+        want, _ = o.render_viewport(vp_dict(vps[k]), W, H, threads=8)
+        assert np.array_equal(got[k], want), k
