@@ -211,7 +211,15 @@ def cpu_cast_rate(tree, origins, dirs, target_s, threads, **cast_args):
     t0 = time.perf_counter()
     tree.cast(so, sd, threads=threads, **cast_args)
     dt = time.perf_counter() - t0
-    return len(so) / dt, len(so), step, dt
+    reps = 1
+    # a whole batch that takes the CPU less than the target is cast again until the target is reached
+    if step == 1 and dt < target_s:
+        more = int(min(1000, target_s / max(dt, 1e-6)))
+        t0 = time.perf_counter()
+        for _ in range(more):
+            tree.cast(so, sd, threads=threads, **cast_args)
+        dt, reps = time.perf_counter() - t0, more
+    return reps * len(so) / dt, reps * len(so), step, dt
 
 
 def batched_variants(svo, torch, scene, rp, hp, n, stream, args, row=0):

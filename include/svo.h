@@ -206,10 +206,11 @@ svo_status svo_cast(svo_scene* scene, const svo_rays* rays, uint64_t n, const sv
  * svo_cast.  Device buffers, the same work queue as svo_cast. */
 svo_status svo_cast_lod(svo_scene* scene, const svo_rays* rays, uint64_t n, const svo_hits* hits, float viewing_distance,
                         void* stream);
-/* Same cast with host ray and hit buffers, stream synchronised before return.  Where the device
- * reads host memory through the CPU's page tables (Grace) the kernel reads the rays and writes the
- * hits in place; elsewhere the batch is staged in chunks through a per-scene device workspace that
- * grows on demand, copies overlapping the casts (with pinned host memory). */
+/* Same cast with host ray and hit buffers, stream synchronised before return.  The batch is staged
+ * in chunks through a per-scene device workspace that grows on demand, copies overlapping the casts
+ * (with pinned host memory); camera images given with their row length (svo_cast_host_rows) are
+ * read and written in place where the device reads host memory through the CPU's page tables
+ * (Grace), see svo_set_host_transfer. */
 svo_status svo_cast_host(svo_scene* scene, const svo_rays* rays, uint64_t n, const svo_hits* hits, void* stream);
 /* The three casts above for rays laid out as rows of row_length rays (a camera image in raster
  * order, or several images one after the other): the work queue hands each warp 8 neighbouring rays
@@ -379,9 +380,10 @@ svo_status svo_selftest_luts(uint64_t* ray_to_node, uint32_t* octant_step, uint6
  * same results; mode 1 exists so tests can check that. */
 svo_status svo_set_cast_mode(int32_t mode);
 /* How svo_cast_host moves rays and hits (process-wide): 0 (default) lets the kernel read and write
- * the host buffers in place when the device accesses host memory through the CPU's page tables
- * (Grace systems) and stages copies elsewhere; 1 always stages copies (chunks over three streams);
- * 2 always accesses host memory directly (an error where the device cannot). */
+ * the host buffers in place for batches with a row layout (svo_cast_host_rows, row_length >= 16)
+ * when the device accesses host memory through the CPU's page tables (Grace systems), and stages
+ * copies otherwise; 1 always stages copies (chunks over three streams); 2 always accesses host
+ * memory directly (an error where the device cannot). */
 svo_status svo_set_host_transfer(int32_t mode);
 
 #ifdef __cplusplus

@@ -668,6 +668,9 @@ svo_status svo_cast_host_rows(svo_scene* sc, const svo_rays* rays, uint64_t n, u
   // Where the device reads host memory through the CPU's page tables (Grace: NVLink-C2C with
   // address translation), the kernel reads the rays and writes the hits in place; elsewhere the
   // batch goes through staged copies.
+  // By default only batches with a row layout (camera images) are read in place: the work queue
+  // casts the rays that enter the octree out of order (packed into full warps), and where many rays
+  // miss the octree their hits would reach host memory in small scattered pieces.
   int direct = 0;
   if (g_host_transfer != 1) {
     int dev = 0;
@@ -675,6 +678,7 @@ svo_status svo_cast_host_rows(svo_scene* sc, const svo_rays* rays, uint64_t n, u
     SVO_CUDA_TRY(cudaDeviceGetAttribute(&direct, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev));
     if (g_host_transfer == 2 && !direct)
       return fail(SVO_ERR_ARGUMENT, "svo_cast_host: this device cannot access host memory directly");
+    if (g_host_transfer == 0 && row_length < 16) direct = 0;
   }
   if (!direct) return cast_host_pipelined(sc, rays, n, hits, st, row_length);
   const svo_status rc = launch_cast(sc, rays, n, hits, st, row_length, true);
