@@ -14,6 +14,7 @@
 #include <string>
 
 #include "svo_internal.h"
+#include "svo_lod.h"
 #include "svo_restart.h"
 
 namespace svo {
@@ -468,15 +469,6 @@ __device__ void cast_ray(const SceneView& s, const SharedLuts& L, float ox, floa
   }
 }
 
-
-// The MIP condition of get_by_ray_at_lod (:366-375): level < (origin - round(p / 2 level) * 2 level).length()
-// / viewing_distance, in the reference's f32 operations.
-__device__ __forceinline__ bool lod_reads_mip(float ox, float oy, float oz, float px, float py, float pz, float level,
-                                              float viewing_distance) {
-  const float m2 = level * 2.0f;
-  const float ax = ox - roundf(px / m2) * m2, ay = oy - roundf(py / m2) * m2, az = oz - roundf(pz / m2) * m2;
-  return level < sqrtf((ax * ax + ay * ay) + az * az) / viewing_distance;
-}
 
 // True when no restart visit from the next one on can read a MIP: the visit after j nudges has
 // level L + j - 1 (L > 0, each visit POPs) and point p_j with |o - p_j| <= |o - p| + j g, g = |c| plus
