@@ -107,6 +107,8 @@ uint32_t BrickArena::alloc() {
     s = (uint32_t)live_.size();
     live_.push_back(0);
     dirty_.push_back(0);
+    hint_.push_back(0);
+    hint_.push_back(0);
     data_.resize(data_.size() + len_);
   }
   live_[s] = 1;
@@ -385,8 +387,13 @@ bool HostOctree::brick_homogeneous(const BrickRef& b, uint32_t* out) const {
   }
   const uint32_t* v = arena.at(b.v);
   const uint32_t first = v[0];
+  uint32_t& hint = arena.differs_at(b.v);  // most bricks stay mixed across the checks of many inserts
+  if (hint < arena.len() && v[hint] != first) return false;
   for (uint32_t i = 1; i < arena.len(); ++i)
-    if (v[i] != first) return false;
+    if (v[i] != first) {
+      hint = i;
+      return false;
+    }
   *out = first;
   return true;
 }
@@ -897,38 +904,55 @@ bool HostOctree::simplify(uint64_t k) {
         store(k, std::move(u));
         return true;
       }
+      // Leaf -> UniformLeaf when every brick downsamples losslessly (:860-995): first the test
+      // alone (it fails for most leaves), then the downsampled brick
       const uint32_t D = dim, half = D / 2;
-      unified_.assign(arena.len(), kEmpty32);
-      uint32_t* uv = unified_.data();
       bool uniform = true;
       for (uint32_t o = 0; o < 8 && uniform; ++o) {
-        const uint64_t ox = round_usize(off_x(o) * (float)half), oy = round_usize(off_y(o) * (float)half),
-                       oz = round_usize(off_z(o) * (float)half);
         const BrickRef& b = bricks[k * 8 + o];
-        if (b.kind == kBrickEmpty) {
+        if (b.kind != kBrickParted) {
           uniform &= brick_equal(b, bricks[k * 8]);
-        } else if (b.kind == kBrickSolid) {
-          uniform &= brick_equal(b, bricks[k * 8]);
-          for (uint64_t x = ox; x < ox + half; ++x)
-            for (uint64_t y = oy; y < oy + half; ++y)
-              for (uint64_t z = oz; z < oz + half; ++z) uv[flat3(x, y, z, D)] = b.v;
-        } else {
-          const uint32_t* v = arena.at(b.v);
-          for (uint64_t x = 0; x < half && uniform; ++x)
-            for (uint64_t y = 0; y < half && uniform; ++y)
-              for (uint64_t z = 0; z < half && uniform; ++z) {
-                const uint32_t c = v[flat3(x * 2, y * 2, z * 2, D)];
-                if (c == v[flat3(x * 2 + 1, y * 2, z * 2, D)] && c == v[flat3(x * 2, y * 2 + 1, z * 2, D)] &&
-                    c == v[flat3(x * 2, y * 2, z * 2 + 1, D)] && c == v[flat3(x * 2 + 1, y * 2 + 1, z * 2, D)] &&
-                    c == v[flat3(x * 2, y * 2 + 1, z * 2 + 1, D)] && c == v[flat3(x * 2 + 1, y * 2, z * 2 + 1, D)] &&
-                    c == v[flat3(x * 2 + 1, y * 2 + 1, z * 2 + 1, D)])
-                  uv[flat3(ox + x, oy + y, oz + z, D)] = c;
-                else
-                  uniform = false;
-              }
+          continue;
         }
+        const uint32_t* v = arena.at(b.v);
+        auto cell_uniform = [&](uint64_t x, uint64_t y, uint64_t z) {
+          const uint32_t c = v[flat3(x * 2, y * 2, z * 2, D)];
+          return c == v[flat3(x * 2 + 1, y * 2, z * 2, D)] && c == v[flat3(x * 2, y * 2 + 1, z * 2, D)] &&
+                 c == v[flat3(x * 2, y * 2, z * 2 + 1, D)] && c == v[flat3(x * 2 + 1, y * 2 + 1, z * 2, D)] &&
+                 c == v[flat3(x * 2, y * 2 + 1, z * 2 + 1, D)] && c == v[flat3(x * 2 + 1, y * 2, z * 2 + 1, D)] &&
+                 c == v[flat3(x * 2 + 1, y * 2 + 1, z * 2 + 1, D)];
+        };
+        uint32_t& hint = arena.mixed_cell(b.v);  // most bricks stay mixed across the checks of many inserts
+        if (hint < half * half * half && !cell_uniform(hint % half, (hint / half) % half, hint / (half * half))) {
+          uniform = false;
+          continue;
+        }
+        for (uint64_t x = 0; x < half && uniform; ++x)
+          for (uint64_t y = 0; y < half && uniform; ++y)
+            for (uint64_t z = 0; z < half && uniform; ++z)
+              if (!cell_uniform(x, y, z)) {
+                uniform = false;
+                hint = (uint32_t)(x + half * (y + half * z));
+              }
       }
       if (uniform) {
+        unified_.assign(arena.len(), kEmpty32);
+        uint32_t* uv = unified_.data();
+        for (uint32_t o = 0; o < 8; ++o) {
+          const uint64_t ox = round_usize(off_x(o) * (float)half), oy = round_usize(off_y(o) * (float)half),
+                         oz = round_usize(off_z(o) * (float)half);
+          const BrickRef& b = bricks[k * 8 + o];
+          if (b.kind == kBrickSolid) {
+            for (uint64_t x = ox; x < ox + half; ++x)
+              for (uint64_t y = oy; y < oy + half; ++y)
+                for (uint64_t z = oz; z < oz + half; ++z) uv[flat3(x, y, z, D)] = b.v;
+          } else if (b.kind == kBrickParted) {
+            const uint32_t* v = arena.at(b.v);
+            for (uint64_t x = 0; x < half; ++x)
+              for (uint64_t y = 0; y < half; ++y)
+                for (uint64_t z = 0; z < half; ++z) uv[flat3(ox + x, oy + y, oz + z, D)] = v[flat3(x * 2, y * 2, z * 2, D)];
+          }
+        }
         const uint32_t slot = arena.alloc();
         std::memcpy(arena.at(slot), unified_.data(), sizeof(uint32_t) * arena.len());
         Content u;

@@ -56,6 +56,10 @@ class BrickArena {
   uint32_t clone(uint32_t slot);
   void release(uint32_t slot);
   uint32_t* at(uint32_t slot) { return &data_[(size_t)slot * len_]; }
+  // an index whose voxel differed from voxel 0 when last looked at (a hint: checked before use)
+  uint32_t& differs_at(uint32_t slot) const { return hint_[2 * (size_t)slot]; }
+  // a 2x2x2 cell (at half resolution, x + y H + z H^2) that was not uniform when last looked at
+  uint32_t& mixed_cell(uint32_t slot) const { return hint_[2 * (size_t)slot + 1]; }
   const uint32_t* at(uint32_t slot) const { return &data_[(size_t)slot * len_]; }
   uint32_t len() const { return len_; }
   uint32_t slots() const { return (uint32_t)live_.size(); }
@@ -70,6 +74,7 @@ class BrickArena {
  private:
   uint32_t len_ = 0;
   std::vector<uint32_t> data_;
+  mutable std::vector<uint32_t> hint_;
   std::vector<uint8_t> live_, dirty_;
   std::vector<uint32_t> free_;
   uint64_t live_count_ = 0;
