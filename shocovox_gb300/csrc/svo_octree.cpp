@@ -1008,11 +1008,9 @@ int HostOctree::insert_at_lod(bool overwrite, const uint32_t up[3], uint32_t isz
     default: none = transparent(data.rgba) && data.user == 0;
   }
   if (none) return 0;
-  struct Frame {
-    uint32_t key;
-    Cube b;
-  };
-  std::vector<Frame> stack{{0u, root}};
+  std::vector<PathFrame>& stack = path_;  // reused: no allocation per operation
+  stack.clear();
+  stack.push_back({0u, root});
   size_t actual = 0;
   const uint32_t target = add_to_palette(data);
   for (;;) {
@@ -1112,11 +1110,9 @@ int HostOctree::clear_at_lod(const uint32_t up[3], uint32_t csz) {
   const Cube root{0.0f, 0.0f, 0.0f, (float)size};
   const float px = (float)up[0], py = (float)up[1], pz = (float)up[2];
   if (!contains(root, px, py, pz)) return 4;
-  struct Frame {
-    uint32_t key;
-    Cube b;
-  };
-  std::vector<Frame> stack{{0u, root}};
+  std::vector<PathFrame>& stack = path_;  // reused: no allocation per operation
+  stack.clear();
+  stack.push_back({0u, root});
   size_t actual = 0;
   for (;;) {
     const size_t cur = stack.back().key;
@@ -1172,9 +1168,9 @@ int HostOctree::clear_at_lod(const uint32_t up[3], uint32_t csz) {
   }
   // post-processing (clear.rs:224-339)
   bool have_removed = false;
-  Frame removed{0, Cube{0, 0, 0, 0}};
+  PathFrame removed{0, Cube{0, 0, 0, 0}};
   if (!stack.empty()) {
-    Frame last = stack.back();
+    PathFrame last = stack.back();
     stack.pop_back();
     if (sat_usize(last.b.size) <= actual) {
       have_removed = true;
@@ -1218,7 +1214,7 @@ int HostOctree::clear_at_lod(const uint32_t up[3], uint32_t csz) {
       deallocate_children_of(k);
       set_children_none(k);
       have_removed = true;
-      removed = Frame{k, nb};
+      removed = PathFrame{k, nb};
       store(k, Content{});
     }
     if (bits == 0)

@@ -142,6 +142,11 @@ class HostOctree {
   int depth_ = 0;
   std::vector<uint32_t> unified_;     // scratch brick of simplify()
   std::vector<uint32_t> dilute_src_;  // scratch copy of dilute()'s source brick
+  struct PathFrame {
+    uint32_t key;
+    Cube b;
+  };
+  std::vector<PathFrame> path_;       // scratch: the nodes an insert or clear walks down
   std::unordered_map<uint32_t, uint32_t> color_index_, data_index_;
 
   // pool (src/object_pool.rs:151-240)
