@@ -127,6 +127,13 @@ svo_status svo_clear(svo_scene* scene, uint32_t x, uint32_t y, uint32_t z);
 svo_status svo_clear_at_lod(svo_scene* scene, uint32_t x, uint32_t y, uint32_t z, uint32_t clear_size);
 /* Applies a recipe of operations in order; *n_done receives how many succeeded. */
 svo_status svo_apply_ops(svo_scene* scene, const svo_op* ops, uint64_t n, uint64_t* n_done);
+/* Bulk insert of a dense w x h x d block at (x0, y0, z0): voxel (x0 + i, y0 + j, z0 + k) receives
+ * rgba[i + w (j + h k)] as its albedo and user[...] as its user data (either array may be NULL, not
+ * both), inserted in the nesting of the reference's fill loops (i outermost, k innermost,
+ * src/raytracing/tests.rs:693-713) exactly as that many Octree::insert calls; an entry without
+ * albedo (alpha 0) or user data (0) inserts nothing.  *n_done receives the number of inserts made. */
+svo_status svo_insert_dense(svo_scene* scene, uint32_t x0, uint32_t y0, uint32_t z0, uint32_t w, uint32_t h, uint32_t d,
+                            const uint32_t* rgba, const uint32_t* user, uint64_t* n_done);
 /* Octree::get (src/octree/mod.rs:416-422) */
 svo_status svo_get(svo_scene* scene, uint32_t x, uint32_t y, uint32_t z, uint32_t* kind, uint32_t* rgba, uint32_t* user);
 svo_status svo_scene_stats_get(svo_scene* scene, svo_scene_stats* out);

@@ -161,6 +161,21 @@ class Octree:
     def clear_at_lod(self, pos, size):
         return self._op(lib().svo_clear_at_lod(self._h, pos[0], pos[1], pos[2], size))
 
+    def insert_dense(self, origin, rgba=None, user=None):
+        """Bulk insert of a dense block: `rgba` and/or `user` are uint32 arrays of shape (d, h, w)
+        (index [k, j, i] for voxel origin + (i, j, k)), inserted like the reference's fill loops."""
+        a = np.ascontiguousarray(rgba, dtype=np.uint32) if rgba is not None else None
+        u = np.ascontiguousarray(user, dtype=np.uint32) if user is not None else None
+        shape = (a if a is not None else u).shape
+        d, h, w = shape
+        done = ctypes.c_uint64()
+        rc = lib().svo_insert_dense(self._h, origin[0], origin[1], origin[2], w, h, d,
+                                    _vp(a.ctypes.data) if a is not None else None,
+                                    _vp(u.ctypes.data) if u is not None else None, ctypes.byref(done))
+        if rc not in (0,):
+            raise OctreeError(rc, "%s (after %d inserts)" % (lib().svo_last_error().decode(), done.value))
+        return done.value
+
     def apply_ops(self, ops):
         ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
         done = ctypes.c_uint64()

@@ -98,6 +98,7 @@ SIGNATURES = {
     "svo_clear": (_I32, [_VP, _U32, _U32, _U32]),
     "svo_clear_at_lod": (_I32, [_VP, _U32, _U32, _U32, _U32]),
     "svo_apply_ops": (_I32, [_VP, _VP, _U64, _P(_U64)]),
+    "svo_insert_dense": (_I32, [_VP, _U32, _U32, _U32, _U32, _U32, _U32, _VP, _VP, _P(_U64)]),
     "svo_get": (_I32, [_VP, _U32, _U32, _U32, _P(_U32), _P(_U32), _P(_U32)]),
     "svo_scene_stats_get": (_I32, [_VP, _P(SceneStats)]),
     "svo_node_record": (_I32, [_VP, _U64, _P(_U64)]),

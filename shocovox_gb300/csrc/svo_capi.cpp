@@ -224,6 +224,26 @@ svo_status svo_apply_ops(svo_scene* s, const svo_op* ops, uint64_t n, uint64_t* 
   return rc;
 }
 
+svo_status svo_insert_dense(svo_scene* s, uint32_t x0, uint32_t y0, uint32_t z0, uint32_t w, uint32_t h, uint32_t d,
+                            const uint32_t* rgba, const uint32_t* user, uint64_t* n_done) {
+  if (!s || (!rgba && !user)) return fail(SVO_ERR_ARGUMENT, "svo_insert_dense: NULL argument");
+  uint64_t done = 0;
+  svo_status rc = SVO_OK;
+  // the nesting of the reference's fill loops: x outermost, z innermost
+  for (uint32_t i = 0; i < w && rc == SVO_OK; ++i)
+    for (uint32_t j = 0; j < h && rc == SVO_OK; ++j)
+      for (uint32_t k = 0; k < d; ++k) {
+        const uint64_t f = (uint64_t)i + (uint64_t)w * ((uint64_t)j + (uint64_t)h * k);
+        const uint32_t c = rgba ? rgba[f] : 0, u = user ? user[f] : 0;
+        const uint32_t kind = (rgba ? SVO_ENTRY_VISUAL : 0) | (user ? SVO_ENTRY_INFORMATIVE : 0);
+        rc = svo_insert(s, x0 + i, y0 + j, z0 + k, kind, c, u);
+        if (rc != SVO_OK) break;
+        ++done;
+      }
+  if (n_done) *n_done = done;
+  return rc;
+}
+
 svo_status svo_get(svo_scene* s, uint32_t x, uint32_t y, uint32_t z, uint32_t* kind, uint32_t* rgba, uint32_t* user) {
   if (!s) return fail(SVO_ERR_ARGUMENT, "NULL scene");
   const uint32_t p[3] = {x, y, z};

@@ -113,3 +113,36 @@ def test_random_update_sequences(oracle_mod, seed, size, dim):
         compare(o, p)
         for pos in rng.integers(0, size, size=(20, 3)):
             assert o.get(tuple(int(v) for v in pos)) == p.get(tuple(int(v) for v in pos))
+
+
+def test_insert_dense_equals_the_reference_fill_loops(oracle_mod):
+    # svo_insert_dense: one Octree::insert per voxel in the nesting of the reference's fill loops
+    # (x outermost, z innermost); empty entries insert nothing; a block past the octree stops with
+    # InvalidPosition after the inserts that fit
+    import shocovox_gb300 as svo
+    from helpers import ALBEDO, COMPLEX, DATA, INSERT, ops_from
+    rng = np.random.default_rng(41)
+    for size, dim, origin, shape, which in ((32, 2, (3, 5, 1), (7, 9, 6), "rgba"), (64, 4, (10, 0, 20), (12, 5, 17), "both"),
+                                            (16, 1, (0, 0, 0), (16, 16, 16), "user")):
+        d, h, w = shape
+        rgba = rng.choice([0, 0x10203000, 0xFF0000FF, 0x00FF00FF, 0x336699FF], size=shape).astype(np.uint32)
+        user = rng.choice([0, 1, 7, 4096], size=shape).astype(np.uint32)
+        a = rgba if which in ("rgba", "both") else None
+        u = user if which in ("user", "both") else None
+        kind = {"rgba": ALBEDO, "user": DATA, "both": COMPLEX}[which]
+        recs = []
+        for i in range(w):
+            for j in range(h):
+                for k in range(d):
+                    recs.append((INSERT, origin[0] + i, origin[1] + j, origin[2] + k, kind,
+                                 int(rgba[k, j, i]) if a is not None else 0, int(user[k, j, i]) if u is not None else 0))
+        o = oracle_mod.Tree(size, dim)
+        o.apply_ops(ops_from(recs))
+        p = svo.Octree(size, dim)
+        assert p.insert_dense(origin, rgba=a, user=u) == w * h * d
+        assert [list(r) for r in p.records()] == [list(r) for r in o.records()], (size, dim, which)
+        assert list(p.palette(0)) == list(o.palette(0)) and list(p.palette(1)) == list(o.palette(1))
+    p = svo.Octree(16, 2)
+    with pytest.raises(svo.OctreeError) as e:
+        p.insert_dense((10, 10, 10), rgba=np.full((8, 8, 8), 0xFF0000FF, np.uint32))
+    assert e.value.code == 4 and "after 6 inserts" in str(e.value)  # z = 16 is the first voxel outside
