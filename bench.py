@@ -118,15 +118,16 @@ class ClockSampler:
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, interval_ms=200):
         self.gpu = str(gpu_index)
+        self.interval_ms = str(interval_ms)
         self.proc = None
         self.lines = []
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", self.gpu, "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", self.interval_ms],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             threading.Thread(target=self._read, daemon=True).start()
         except (OSError, ValueError):
@@ -525,10 +526,12 @@ def run_served(args, w):
                 "launches": st["launches"], "uploads": st["uploads"], "evictions": st["evictions"],
                 "mean_batch": round(float(np.mean([x["batch_requests"] for x in res])), 2)}
 
-    clocks = ClockSampler(0)
+    # latency-bound: clock samples once a second (each nvidia-smi query is a driver call on the host)
+    clocks = ClockSampler(0, interval_ms=1000)
     clocks.start()
     budget = int(w["budget_gb"] * (1 << 30))
-    batched = serve(svo.Server(budget_bytes=budget, max_batch_requests=64, max_batch_rays=1 << 25, max_inflight=3),
+    # paced load: launches of at most 4 M rays keep a large request from delaying the next ones
+    batched = serve(svo.Server(budget_bytes=budget, max_batch_requests=64, max_batch_rays=1 << 22, max_inflight=3),
                     paced=True)
     serial = serve(svo.Server(budget_bytes=budget, max_batch_requests=1, max_inflight=1), paced=True)
     # capacity: the same requests submitted as fast as result buffers free up (48 in flight)
@@ -543,6 +546,9 @@ def run_served(args, w):
         "config": {"workload": "served16", "scenes": len(scenes), "sizes": sizes, "requests": n_req,
                    "arrival_rate_per_s": w["rate"], "rays": total_rays, "budget_gb": w["budget_gb"],
                    "build_s": round(build_s, 1), "outputs": "status + albedo per ray, to pinned host memory",
+                   "server_config": {"paced": "max_batch_requests 64, max_batch_rays 2^22, max_inflight 3",
+                                     "capacity": "max_batch_requests 64, max_batch_rays 2^25, max_inflight 3",
+                                     "serial_dispatch": "max_batch_requests 1, max_inflight 1"},
                    "served": batched, "serial_dispatch": serial,
                    "capacity": {"note": "all requests queued, 48 outstanding", "served": batched_cap,
                                 "serial_dispatch": serial_cap},
