@@ -40,8 +40,8 @@ __global__ void __launch_bounds__(128, 7) cast_kernel(SceneView s, RaysView rays
 // enter is cast as it is; the entering rays of other claims wait in the warp's slice of shared
 // memory, with the point where they enter, until 32 of them fill the warp, so that rays from
 // outside the octree (most of them missing it) do not leave most lanes idle.
-struct WaitingRays {
-  float o[3][64], d[3][64], p[3][64];
+struct WaitingRays {  // the ray's origin and direction are read again from the ray arrays
+  float p[3][64];
   uint32_t target[64];  // octant of the entry point; bit 31: fast form
   unsigned long long i[64];
 };
@@ -97,12 +97,6 @@ __global__ void __launch_bounds__(128, 7)
       }
       if (enters) {
         const uint32_t k = count + __popc(m & ((1u << lane) - 1u));
-        w.o[0][k] = ox;
-        w.o[1][k] = oy;
-        w.o[2][k] = oz;
-        w.d[0][k] = dx;
-        w.d[1][k] = dy;
-        w.d[2][k] = dz;
         w.p[0][k] = px;
         w.p[1][k] = py;
         w.p[2][k] = pz;
@@ -117,18 +111,18 @@ __global__ void __launch_bounds__(128, 7)
       const uint32_t take = count < 32 ? count : 32;
       if (lane < take) {
         const uint32_t k = count - take + lane;
-        ox = w.o[0][k];
-        oy = w.o[1][k];
-        oz = w.o[2][k];
-        dx = w.d[0][k];
-        dy = w.d[1][k];
-        dz = w.d[2][k];
+        i = w.i[k];
+        ox = __ldg(rays.ox + i);
+        oy = __ldg(rays.oy + i);
+        oz = __ldg(rays.oz + i);
+        dx = __ldg(rays.dx + i);
+        dy = __ldg(rays.dy + i);
+        dz = __ldg(rays.dz + i);
         px = w.p[0][k];
         py = w.p[1][k];
         pz = w.p[2][k];
         target = w.target[k] & 0x7FFFFFFFu;
         fast = (w.target[k] >> 31) != 0u;
-        i = w.i[k];
         have = true;
       }
       count -= take;
