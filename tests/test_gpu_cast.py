@@ -312,8 +312,16 @@ def test_row_layout_casts_equal_plain_casts(oracle_mod):
     for m in (n - 37, 4 * W * 9 + 5, 20000):  # partial last band; below the work-queue size
         same(device_cast(m, W), {k: v[:m] for k, v in plain.items()}, "rows %d, n %d" % (W, m))
     # host buffers: in place (Grace) and staged in chunks of whole bands
-    # (with and without counters: the instrumented cast is a kernel of its own)
+    # (with and without counters: the instrumented cast is a kernel of its own; mode 2 reads host
+    # memory in place even without a row layout, where the device can)
     no_counters = [k for k in svo.HIT_FIELDS if k not in COUNTERS + ["run_visits"]]
+    if svo.lib().svo_set_host_transfer(2) == 0:
+        try:
+            same(p.cast_host(origins, dirs), plain, "host in place, plain order")
+            same(p.cast_host(origins, dirs, fields=no_counters, row_length=W), {k: plain[k] for k in no_counters},
+                 "host in place, rows")
+        finally:
+            svo.lib().svo_set_host_transfer(0)
     for mode in (0, 1):
         assert svo.lib().svo_set_host_transfer(mode) == 0
         try:
