@@ -763,7 +763,7 @@ def run_viewport(args, w):
                                                    "ms_per_step": round(cast_frames_ms, 4),
                                                    "note": "the same, one launch per frame like the render"}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_src,
+                     "frac": round(achieved / peak, 4), "traffic": profile_traffic(args.workload).get("dram_bytes_per_launch"), "peak_source": peak_src,
                      "alg_bytes_per_launch": alg, "alg_bytes_per_ray": round(alg / n, 2)},
         "cpu_baseline": cpu,
         "e2e": {"value": round(n / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
@@ -894,7 +894,7 @@ def run_lod(args, w):
                    "svo_cast_lod_plain_order": {"value": round(n / (lod_plain_order_ms / 1e3) / 1e6, 3),
                                                 "ms_per_step": round(lod_plain_order_ms, 4)}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_src,
+                     "frac": round(achieved / peak, 4), "traffic": profile_traffic(args.workload).get("dram_bytes_per_launch"), "peak_source": peak_src,
                      "alg_bytes_per_launch": alg, "alg_bytes_per_ray": round(alg / n, 2)},
         "cpu_baseline": cpu,
         "e2e": {"value": round(n / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": n * 24,
