@@ -243,13 +243,15 @@ def batched_variants(svo, torch, scene, rp, hp, n, stream, args, row=0):
     sweep = []
     for block in (64, 96, 128):
         for chunk in (32, 64, 256):
-            cfg = svo.LaunchConfig(block, chunk, 0, 0)
-            sweep.append(((block, chunk), timed(cfg, 2)))
-    (block, chunk), _ = min(sweep, key=lambda t: t[1])
-    ms = timed(svo.LaunchConfig(block, chunk, 0, 0), args.steps)
+            for shape in ((3, 4) if row else (0,)):
+                cfg = svo.LaunchConfig(block, chunk, 0, shape)
+                sweep.append(((block, chunk, shape), timed(cfg, 2)))
+    (block, chunk, shape), _ = min(sweep, key=lambda t: t[1])
+    ms = timed(svo.LaunchConfig(block, chunk, 0, shape), args.steps)
     return {"persistent_autotuned": {"value": round(n / (ms / 1e3) / 1e6, 3), "unit": "Mrays/s",
-                                     "ms_per_step": round(ms, 4), "block": block, "rays_per_chunk": chunk},
-            "sweep_ms": {"%dx%d" % k: round(v, 3) for k, v in sweep}}
+                                     "ms_per_step": round(ms, 4), "block": block, "rays_per_chunk": chunk,
+                                     "block_shape": shape},
+            "sweep_ms": {"%dx%dx%d" % k: round(v, 3) for k, v in sweep}}
 
 
 def multiscene_specs(w):
@@ -368,7 +370,7 @@ def run_multiscene(args, w):
     # one persistent launch captured in a CUDA graph (workspace already sized, blocks per SM fixed)
     if cfg.blocks_per_sm == 0:
         per_sm = {64: 14, 96: 9, 128: 7}.get(cfg.block, 2)  # resident blocks at 72 registers per thread
-        gcfg = svo.LaunchConfig(cfg.block, cfg.rays_per_chunk, per_sm, 0)
+        gcfg = svo.LaunchConfig(cfg.block, cfg.rays_per_chunk, per_sm, cfg.block_shape)
     else:
         gcfg = cfg
     gstream = torch.cuda.Stream(dev)

@@ -278,7 +278,8 @@ typedef struct {
   uint32_t block;          /* threads per block (multiple of 32, <= 128); 0 = default 128 */
   uint32_t rays_per_chunk; /* rays a warp claims per work-queue grab; 0 = default 64 */
   uint32_t blocks_per_sm;  /* persistent CTAs per SM; 0 = default from occupancy */
-  uint32_t reserved;
+  uint32_t block_shape;    /* rays of an item with a row length cast together: 0 or 3 = 8 x 4, 4 = 16 x 2,
+                              5 = 32 x 1 (log2 of the width) */
 } svo_launch_config;
 
 /* Casts every item's rays in one persistent kernel launch driven by a device

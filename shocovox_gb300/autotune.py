@@ -1,9 +1,10 @@
 """Autotuner of the persistent batched cast (svo_cast_batched).
 
-Sweeps threads per block, rays per warp grab and persistent CTAs per SM on the
-caller's own batch, keeps the fastest, and caches the choice per (GPU name,
-workload signature) in a JSON file next to the built library, so later runs
-skip the sweep.
+Sweeps threads per block, rays per warp grab, persistent CTAs per SM and, for
+batches with camera images (items with a row length), the shape of the ray
+blocks a warp casts together, on the caller's own batch; keeps the fastest and
+caches the choice per (GPU name, workload signature) in a JSON file next to the
+built library, so later runs skip the sweep.
 """
 import json
 import os
@@ -15,6 +16,7 @@ CACHE = os.path.join(os.path.dirname(_lib.lib_path()), "autotune_cache.json")
 BLOCKS = (64, 96, 128)
 CHUNKS = (32, 64, 128)
 PER_SM = (0,)  # 0 = as many as occupancy allows
+SHAPES = (3, 4)  # ray blocks of 8 x 4 or 16 x 2 for items with a row length
 
 
 def _load():
@@ -46,18 +48,19 @@ def tune(ws, items, gpu_name, time_fn, use_cache=True):
     key = "%s|%s" % (gpu_name, signature(items))
     cache = _load() if use_cache else {}
     if key in cache:
-        b, c, p = cache[key]["config"]
-        return _lib.LaunchConfig(b, c, p, 0), {"cached": True, **cache[key]}
+        b, c, p, sh = (list(cache[key]["config"]) + [0])[:4]
+        return _lib.LaunchConfig(b, c, p, sh), {"cached": True, **cache[key]}
+    shapes = SHAPES if any(len(it) > 4 and it[4] for it in items) else (0,)
     table = {}
     for b in BLOCKS:
         for c in CHUNKS:
             for p in PER_SM:
-                cfg = _lib.LaunchConfig(b, c, p, 0)
-                table["%dx%dx%d" % (b, c, p)] = time_fn(cfg)
+                for sh in shapes:
+                    table["%dx%dx%dx%d" % (b, c, p, sh)] = time_fn(_lib.LaunchConfig(b, c, p, sh))
     best = min(table, key=table.get)
-    b, c, p = (int(v) for v in best.split("x"))
-    entry = {"config": [b, c, p], "ms": table[best], "sweep_ms": table, "when": time.strftime("%Y-%m-%dT%H:%M:%S")}
+    b, c, p, sh = (int(v) for v in best.split("x"))
+    entry = {"config": [b, c, p, sh], "ms": table[best], "sweep_ms": table, "when": time.strftime("%Y-%m-%dT%H:%M:%S")}
     if use_cache:
         cache[key] = entry
         _store(cache)
-    return _lib.LaunchConfig(b, c, p, 0), {"cached": False, **entry}
+    return _lib.LaunchConfig(b, c, p, sh), {"cached": False, **entry}

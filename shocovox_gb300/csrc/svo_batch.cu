@@ -32,11 +32,11 @@ struct BatchItemDev {
 };
 
 // fills the device form of one item at global index `begin`; returns the indices it spans
-uint64_t item_dev(const svo_batch_item& it, uint64_t begin, BatchItemDev& d) {
+uint64_t item_dev(const svo_batch_item& it, uint64_t begin, uint32_t shape, BatchItemDev& d) {
   d.scene = scene_view(it.scene);
   d.rays = RaysView{it.rays.ox, it.rays.oy, it.rays.oz, it.rays.dx, it.rays.dy, it.rays.dz};
   d.hits = hits_view_of(it.hits);
-  d.order = claim_order(it.n, it.row_length);
+  d.order = claim_order(it.n, it.row_length, shape);
   d.begin = begin;
   d.n = it.n;
   return 32 * d.order.claims;
@@ -254,6 +254,8 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
     // the pinned staging table is reused: wait until its previous upload has left it
     SVO_CUDA_TRY(cudaEventSynchronize(ws->copied));
   }
+  const uint32_t shape = (cfg && cfg->block_shape) ? cfg->block_shape : 3;
+  if (shape < 3 || shape > 5) return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: block_shape must be 0, 3, 4 or 5");
   uint64_t total = 0;
   bool count = false;
   for (uint32_t i = 0; i < n_items; ++i) {
@@ -262,7 +264,7 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
     if (!it.scene->dev.valid) return fail(SVO_ERR_NOT_UPLOADED, "svo_cast_batched: scene not uploaded");
     if (it.n && (!it.rays.ox || !it.rays.oy || !it.rays.oz || !it.rays.dx || !it.rays.dy || !it.rays.dz))
       return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: NULL ray array");
-    total += item_dev(it, total, ws->h_items[i]);
+    total += item_dev(it, total, shape, ws->h_items[i]);
     count |= counts_requested(it.hits);
   }
   if (total == 0) return SVO_OK;
@@ -352,6 +354,9 @@ svo_status svo_cast_batched_noalloc(const svo_batch_item* items, uint32_t n_item
   if (rc != SVO_OK) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   BatchItemDev table[kNoAllocMaxItems];
+  const uint32_t shape = (cfg && cfg->block_shape) ? cfg->block_shape : 3;
+  if (shape < 3 || shape > 5)
+    return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: block_shape must be 0, 3, 4 or 5");
   uint64_t total = 0;
   bool count = false;
   for (uint32_t i = 0; i < n_items; ++i) {
@@ -360,7 +365,7 @@ svo_status svo_cast_batched_noalloc(const svo_batch_item* items, uint32_t n_item
     if (!it.scene->dev.valid) return fail(SVO_ERR_NOT_UPLOADED, "svo_cast_batched_noalloc: scene not uploaded");
     if (it.n && (!it.rays.ox || !it.rays.oy || !it.rays.oz || !it.rays.dx || !it.rays.dy || !it.rays.dz))
       return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: NULL ray array");
-    total += item_dev(it, total, table[i]);
+    total += item_dev(it, total, shape, table[i]);
     count |= counts_requested(it.hits);
   }
   if (total == 0) return SVO_OK;

@@ -262,7 +262,10 @@ def test_batched_multi_scene_matches_single_scene_casts(oracle_mod):
         scenes.append(p)
         keep.append((cols, out))
     ws = svo.BatchWorkspace()
-    for cfg in (svo.LaunchConfig(0, 0, 0, 0), svo.LaunchConfig(128, 32, 1, 0), svo.LaunchConfig(64, 512, 2, 0)):
+    with pytest.raises(Exception):
+        ws.cast(items, svo.LaunchConfig(0, 0, 0, 2), torch.cuda.current_stream().cuda_stream)  # no such block shape
+    for cfg in (svo.LaunchConfig(0, 0, 0, 0), svo.LaunchConfig(128, 32, 1, 0), svo.LaunchConfig(64, 512, 2, 0),
+                svo.LaunchConfig(96, 64, 0, 4), svo.LaunchConfig(128, 32, 0, 5)):
         for _, out in keep:
             for v in out.values():
                 v.zero_()
