@@ -677,7 +677,28 @@ def run_viewport(args, w):
         render()
         pin.copy_(img, non_blocking=True)
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t1) / args.steps
+    e2e_one_s = (time.perf_counter() - t1) / args.steps
+    # the same with two launches of two frames on two streams: one pair's copy overlaps the other's render
+    pair_streams = [torch.cuda.Stream(dev) for _ in range(2)]
+    pair_start = torch.cuda.Event()
+
+    def render_pairs_to_host():
+        pair_start.record(stream)
+        for q, st in enumerate(pair_streams):
+            st.wait_event(pair_start)
+            with torch.cuda.stream(st):
+                scene.render_viewports(vps[2 * q:2 * q + 2], W, H, img[2 * q].data_ptr(), bad.data_ptr(), st.cuda_stream)
+                pin[2 * q:2 * q + 2].copy_(img[2 * q:2 * q + 2], non_blocking=True)
+        for st in pair_streams:
+            stream.wait_stream(st)
+    render_pairs_to_host()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        render_pairs_to_host()
+    torch.cuda.synchronize()
+    e2e_pairs_s = (time.perf_counter() - t1) / args.steps
+    e2e_s = e2e_pairs_s
     # the same frames with one svo_render_viewport call (one launch) per frame
     render_one_per_call()
     torch.cuda.synchronize()
@@ -769,7 +790,9 @@ def run_viewport(args, w):
                      "alg_bytes_per_launch": alg, "alg_bytes_per_ray": round(alg / n, 2)},
         "cpu_baseline": cpu,
         "e2e": {"value": round(n / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": n * 4},
+                "d2h_bytes_per_step": n * 4,
+                "paths": {"one_launch_then_copy": round(n / e2e_one_s / 1e6, 3),
+                          "two_streams_of_two_frames": round(n / e2e_pairs_s / 1e6, 3)}},
         "gpu_launches": args.steps, "clocks": clk,
     }))
 
