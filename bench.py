@@ -244,14 +244,32 @@ def batched_variants(svo, torch, scene, rp, hp, n, stream, args, row=0):
     for block in (64, 96, 128):
         for chunk in (32, 64, 256):
             for shape in ((3, 4) if row else (0,)):
-                cfg = svo.LaunchConfig(block, chunk, 0, shape)
-                sweep.append(((block, chunk, shape), timed(cfg, 2)))
-    (block, chunk, shape), _ = min(sweep, key=lambda t: t[1])
-    ms = timed(svo.LaunchConfig(block, chunk, 0, shape), args.steps)
-    return {"persistent_autotuned": {"value": round(n / (ms / 1e3) / 1e6, 3), "unit": "Mrays/s",
-                                     "ms_per_step": round(ms, 4), "block": block, "rays_per_chunk": chunk,
-                                     "block_shape": shape},
-            "sweep_ms": {"%dx%dx%d" % k: round(v, 3) for k, v in sweep}}
+                for sort in ((0,) if row else (0, 1)):
+                    cfg = svo.LaunchConfig(block, chunk, 0, shape, sort)
+                    sweep.append(((block, chunk, shape, sort), timed(cfg, 2)))
+    (block, chunk, shape, sort), _ = min(sweep, key=lambda t: t[1])
+    ms = timed(svo.LaunchConfig(block, chunk, 0, shape, sort), args.steps)
+    out = {"persistent_autotuned": {"value": round(n / (ms / 1e3) / 1e6, 3), "unit": "Mrays/s",
+                                    "ms_per_step": round(ms, 4), "block": block, "rays_per_chunk": chunk,
+                                    "block_shape": shape, "sort_key": sort,
+                                    "launches_per_step": batched_launches(items, sort)},
+           "sweep_ms": {"%dx%dx%dx%d" % k: round(v, 3) for k, v in sweep}}
+    if not row:
+        # the best of each ray order, timed over K steps
+        for so in (0, 1):
+            (b, c, sh, _), _ = min((t for t in sweep if t[0][3] == so), key=lambda t: t[1])
+            ms = timed(svo.LaunchConfig(b, c, 0, sh, so), args.steps)
+            out["persistent_sort%d" % so] = {"value": round(n / (ms / 1e3) / 1e6, 3), "unit": "Mrays/s",
+                                             "ms_per_step": round(ms, 4), "block": b, "rays_per_chunk": c}
+    return out
+
+
+def batched_launches(items, sort_key):
+    """Kernel launches of one svo_cast_batched call: the claim-order cast if any item is cast in claim
+    order, plus the ray sort's bin, three scan, scatter and cast launches if any item is sorted."""
+    sorted_items = [it for it in items if sort_key and not (len(it) > 4 and it[4]) and it[2]]
+    claimed = [it for it in items if it[2] and it not in sorted_items]
+    return (1 if claimed else 0) + (6 if sorted_items else 0)
 
 
 def multiscene_specs(w):
@@ -370,7 +388,7 @@ def run_multiscene(args, w):
     # one persistent launch captured in a CUDA graph (workspace already sized, blocks per SM fixed)
     if cfg.blocks_per_sm == 0:
         per_sm = {64: 14, 96: 9, 128: 7}.get(cfg.block, 2)  # resident blocks at 72 registers per thread
-        gcfg = svo.LaunchConfig(cfg.block, cfg.rays_per_chunk, per_sm, cfg.block_shape)
+        gcfg = svo.LaunchConfig(cfg.block, cfg.rays_per_chunk, per_sm, cfg.block_shape, cfg.sort_key)
     else:
         gcfg = cfg
     gstream = torch.cuda.Stream(dev)
@@ -487,14 +505,15 @@ def run_multiscene(args, w):
                    "sizes": sorted({sp["size"] for sp in specs}), "brick_dims": sorted({sp["brick_dim"] for sp in specs}),
                    "voxels_inserted": int(sum(b[1] for b in built)), "build_s": round(build_s, 1),
                    "l2": "rays %.0f MB + hits %.0f MB per step (larger than L2)" % (total * 24 / 1e6, total * 34 / 1e6),
-                   "timed": "one persistent batched launch replayed from a CUDA graph",
+                   "timed": "the batched cast replayed from a CUDA graph (one persistent launch; with sort_key 1 the ray sort's six launches too)",
                    "ray_order": "per scene: camera rays as rows of the image (8 x 4 ray blocks per warp), "
-                                "random rays in order",
+                                "random rays in order or sorted by direction octant and entry point (autotune.sort_key)",
                    "serial_plain": {"value": round(total / (serial_ms / 1e3) / 1e6, 3), "ms_per_step": round(serial_ms, 4),
                                     "launches_per_step": len(items)},
                    "batched": {"value": round(total / (batched_ms / 1e3) / 1e6, 3), "ms_per_step": round(batched_ms, 4)},
                    "batched_equals_serial": bool(same),
-                   "autotune": {"block": cfg.block, "rays_per_chunk": cfg.rays_per_chunk, "cached": tune_info["cached"],
+                   "autotune": {"block": cfg.block, "rays_per_chunk": cfg.rays_per_chunk, "block_shape": cfg.block_shape,
+                                "sort_key": cfg.sort_key, "cached": tune_info["cached"],
                                 "sweep_ms": tune_info.get("sweep_ms")}},
         "roofline": {"bound": "hbm", "achieved": round(alg / (graph_ms / 1e3) / 1e9, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(alg / (graph_ms / 1e3) / 1e9 / peak, 4), "traffic": None, "peak_source": peak_src,
@@ -504,7 +523,7 @@ def run_multiscene(args, w):
                 "d2h_bytes_per_step": total * sum(OUT_BYTES.values()),
                 "how": "4 groups of items, each copy-in, batched launch, copy-out on its own stream",
                 "one_stream": round(total / e2e_serial_s / 1e6, 3), "same_hits_as_one_stream": bool(groups_same)},
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * batched_launches(bitems, gcfg.sort_key),
         "clocks": clk,
     }))
 

@@ -280,11 +280,22 @@ typedef struct {
   uint32_t blocks_per_sm;  /* persistent CTAs per SM; 0 = default from occupancy */
   uint32_t block_shape;    /* rays of an item with a row length cast together: 0 or 3 = 8 x 4, 4 = 16 x 2,
                               5 = 32 x 1 (log2 of the width) */
+  uint32_t sort_key;       /* order of the rays of the items without a row length: 0 = index order;
+                              1 = sorted by (item, octant of the direction, Morton code of the point
+                              where the ray enters the octree), so that a warp's rays walk much the
+                              same nodes (svo_cast_batched only: needs the workspace's buffers, which
+                              grow to 128 bytes per such ray) */
 } svo_launch_config;
 
 /* Casts every item's rays in one persistent kernel launch driven by a device
  * work counter.  The per-launch item table and counter live in a workspace
- * owned by `ws` (create it once; it grows only when the item count grows). */
+ * owned by `ws` (create it once; it grows only when the item count grows).
+ * With sort_key 1 the items without a row length are cast through the ray sort
+ * instead: a binning launch (misses written at once), a scan of the bucket
+ * counts, a scatter into bucket order and a persistent cast of the sorted
+ * entering rays, all on `stream`; the hits are the same as in index order.  The
+ * sort's buffers grow only when the rays (or buckets) of a call outgrow them:
+ * make the largest call once before a stream capture. */
 typedef struct svo_batch_workspace svo_batch_workspace;
 svo_status svo_batch_workspace_create(svo_batch_workspace** out);
 void svo_batch_workspace_destroy(svo_batch_workspace* ws);

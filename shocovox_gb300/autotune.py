@@ -1,10 +1,11 @@
 """Autotuner of the persistent batched cast (svo_cast_batched).
 
-Sweeps threads per block, rays per warp grab, persistent CTAs per SM and, for
-batches with camera images (items with a row length), the shape of the ray
-blocks a warp casts together, on the caller's own batch; keeps the fastest and
-caches the choice per (GPU name, workload signature) in a JSON file next to the
-built library, so later runs skip the sweep.
+Sweeps threads per block, rays per warp grab, persistent CTAs per SM, for
+batches with camera images (items with a row length) the shape of the ray
+blocks a warp casts together, and for batches with rays in no particular order
+(items without a row length) the ray-sort key, on the caller's own batch; keeps
+the fastest and caches the choice per (GPU name, workload signature) in a JSON
+file next to the built library, so later runs skip the sweep.
 """
 import json
 import os
@@ -17,6 +18,7 @@ BLOCKS = (64, 96, 128)
 CHUNKS = (32, 64, 128)
 PER_SM = (0,)  # 0 = as many as occupancy allows
 SHAPES = (3, 4)  # ray blocks of 8 x 4 or 16 x 2 for items with a row length
+SORT_KEYS = (0, 1)  # index order, or sorted by direction octant and entry point
 
 
 def _load():
@@ -45,22 +47,25 @@ def signature(items):
 
 def tune(ws, items, gpu_name, time_fn, use_cache=True):
     """Returns (LaunchConfig, table).  time_fn(cfg) -> milliseconds of one batched cast."""
-    key = "%s|%s" % (gpu_name, signature(items))
+    key = "%s|%s|sort" % (gpu_name, signature(items))
     cache = _load() if use_cache else {}
     if key in cache:
-        b, c, p, sh = (list(cache[key]["config"]) + [0])[:4]
-        return _lib.LaunchConfig(b, c, p, sh), {"cached": True, **cache[key]}
+        b, c, p, sh, so = (list(cache[key]["config"]) + [0, 0])[:5]
+        return _lib.LaunchConfig(b, c, p, sh, so), {"cached": True, **cache[key]}
     shapes = SHAPES if any(len(it) > 4 and it[4] for it in items) else (0,)
+    sorts = SORT_KEYS if any(not (len(it) > 4 and it[4]) and it[2] for it in items) else (0,)
     table = {}
     for b in BLOCKS:
         for c in CHUNKS:
             for p in PER_SM:
                 for sh in shapes:
-                    table["%dx%dx%dx%d" % (b, c, p, sh)] = time_fn(_lib.LaunchConfig(b, c, p, sh))
+                    for so in sorts:
+                        table["%dx%dx%dx%dx%d" % (b, c, p, sh, so)] = time_fn(_lib.LaunchConfig(b, c, p, sh, so))
     best = min(table, key=table.get)
-    b, c, p, sh = (int(v) for v in best.split("x"))
-    entry = {"config": [b, c, p, sh], "ms": table[best], "sweep_ms": table, "when": time.strftime("%Y-%m-%dT%H:%M:%S")}
+    b, c, p, sh, so = (int(v) for v in best.split("x"))
+    entry = {"config": [b, c, p, sh, so], "ms": table[best], "sweep_ms": table,
+             "when": time.strftime("%Y-%m-%dT%H:%M:%S")}
     if use_cache:
         cache[key] = entry
         _store(cache)
-    return _lib.LaunchConfig(b, c, p, sh), {"cached": False, **entry}
+    return _lib.LaunchConfig(b, c, p, sh, so), {"cached": False, **entry}

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -32,13 +33,14 @@ struct BatchItemDev {
 };
 
 // fills the device form of one item at global index `begin`; returns the indices it spans
-uint64_t item_dev(const svo_batch_item& it, uint64_t begin, uint32_t shape, BatchItemDev& d) {
+// (none when the item's rays are cast through the ray sort instead: `claimed` false)
+uint64_t item_dev(const svo_batch_item& it, uint64_t begin, uint32_t shape, BatchItemDev& d, bool claimed = true) {
   d.scene = scene_view(it.scene);
   d.rays = RaysView{it.rays.ox, it.rays.oy, it.rays.oz, it.rays.dx, it.rays.dy, it.rays.dz};
   d.hits = hits_view_of(it.hits);
-  d.order = claim_order(it.n, it.row_length, shape);
+  d.n = claimed ? it.n : 0;
+  d.order = claim_order(d.n, it.row_length, shape);
   d.begin = begin;
-  d.n = it.n;
   return 32 * d.order.claims;
 }
 
@@ -185,17 +187,372 @@ __global__ void __launch_bounds__(kBatchMaxBlock, 7)
   }
 }
 
+// ---- ray sort (svo_launch_config.sort_key = 1) -------------------------------------------------
+//
+// The rays of the items without a row length (rays in no particular order, such as rays from random
+// points in random directions) are cast in the order of a key instead of their index order, so that
+// a warp's 32 rays start near one another and head the same way and walk much the same nodes:
+//   1. bin_kernel: a ray that misses its octree's root box gets its miss written at once; an entering
+//      ray gets its bucket (item, octant of its direction, Morton code of its entry point at `bits`
+//      bits an axis), counted into the bucket's count, and is appended, with the point where it
+//      enters, to an unsorted list;
+//   2. the bucket counts are turned into bucket offsets (exclusive scan: scan_reduce, scan_top,
+//      scan_down);
+//   3. scatter_kernel moves every listed ray to the next free place of its bucket (atomicAdd on the
+//      bucket's offset);
+//   4. sorted_cast_kernel casts the sorted list, warps claiming `rays_per_chunk` rays at a time.
+// The order of the rays inside a bucket depends on the atomics' order; a ray's result does not.
+struct SortItemDev {
+  uint64_t begin;         // first index of the item in the sort's index space (plain order)
+  uint64_t n;             // the item's rays in it (0: the item is cast in claim order)
+  uint32_t bucket_base;   // first bucket of the item
+  uint32_t bits;          // bits of the entry point's Morton code per axis
+};
+
+// One entering ray of the sort, 64 bytes (four 16-byte pieces).
+struct __align__(16) SortedRay {
+  float o[3], d[3], p[3];
+  uint32_t target;  // octant of the entry point; bit 31: fast form
+  uint32_t item;
+  uint32_t rank;    // (unused)
+  uint32_t bucket;  // (unsorted list)
+  uint32_t pad;
+  unsigned long long i;  // ray index in the item
+};
+static_assert(sizeof(SortedRay) == 64, "SortedRay is four 16-byte pieces");
+// the kernels read a SortedRay as four float4 (a, b, c, d): o = a.xyz, d = (a.w, b.x, b.y),
+// p = (b.z, b.w, c.x), target = c.y, item = c.z, rank = c.w, bucket = d.x, i = d.zw
+static_assert(offsetof(SortedRay, d) == 12 && offsetof(SortedRay, p) == 24 && offsetof(SortedRay, target) == 36 &&
+                  offsetof(SortedRay, item) == 40 && offsetof(SortedRay, rank) == 44 &&
+                  offsetof(SortedRay, bucket) == 48 && offsetof(SortedRay, i) == 56,
+              "SortedRay layout");
+
+// bits of the entry point's Morton code per axis for an item of n rays: about 16 rays a bucket
+inline uint32_t sort_bits(uint64_t n) {
+  uint32_t len = 0;
+  while (len < 64 && (n >> len)) ++len;
+  const int b = ((int)len - 7) / 3;
+  return (uint32_t)std::min(std::max(b, 0), 6);
+}
+
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {  // bit k of v to bit 3k (v < 2^7)
+  uint32_t r = 0;
+#pragma unroll
+  for (int k = 0; k < 7; ++k) r |= ((v >> k) & 1u) << (3 * k);
+  return r;
+}
+
+constexpr uint32_t kSortBlock = 256;
+
+// The one sorted item of a call whose sort holds a single item: its views ride in the kernel
+// parameters (read from the constant bank) instead of the item table in global memory.
+struct OneItem {
+  SceneView scene;
+  RaysView rays;
+  HitsView hits;
+  SortItemDev sort;
+  uint32_t index;
+};
+
+// Ray j of an item (origin o, direction d): its miss written at once, or its record (with its
+// bucket) in r.
+template <bool kCount>
+__device__ __forceinline__ bool bin_ray(const SceneView& sc, const HitsView& hv, const SortItemDev& si,
+                                        uint32_t item, uint64_t j, const float (&o)[3], const float (&d)[3],
+                                        SortedRay& r) {
+  const float ox = o[0], oy = o[1], oz = o[2], dx = d[0], dy = d[1], dz = d[2];
+  const bool fast = !sc.literal && !isnan(dx) && !isnan(dy) && !isnan(dz);
+  float px = ox, py = oy, pz = oz;
+  uint32_t target = 0;
+  if (fast && !fast_entry(sc, ox, oy, oz, dx, dy, dz, px, py, pz, target)) {
+    HitRecord h;
+    miss_record(h);
+    write_hit(sc, hv, j, h);
+    if (kCount) write_counters(hv, j, h);
+    return false;
+  }
+  // the key: only an order, so any rounding will do (a literal ray keys on its origin)
+  const uint32_t q = 1u << si.bits;
+  const float scale = (float)q * sc.inv_size;
+  const uint32_t qx = (uint32_t)fminf(fmaxf(px * scale, 0.0f), (float)(q - 1));
+  const uint32_t qy = (uint32_t)fminf(fmaxf(py * scale, 0.0f), (float)(q - 1));
+  const uint32_t qz = (uint32_t)fminf(fmaxf(pz * scale, 0.0f), (float)(q - 1));
+  const uint32_t oct = (uint32_t)(dx >= 0.0f) | ((uint32_t)(dy >= 0.0f) << 1) | ((uint32_t)(dz >= 0.0f) << 2);
+  r.o[0] = ox;
+  r.o[1] = oy;
+  r.o[2] = oz;
+  r.d[0] = dx;
+  r.d[1] = dy;
+  r.d[2] = dz;
+  r.p[0] = px;
+  r.p[1] = py;
+  r.p[2] = pz;
+  r.target = target | (fast ? 0x80000000u : 0u);
+  r.item = item;
+  r.bucket = si.bucket_base + (oct << (3 * si.bits)) + (spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2));
+  r.rank = 0;
+  r.pad = 0;
+  r.i = j;
+  return true;
+}
+
+constexpr uint32_t kBinRays = 2;  // rays per lane per round of the binning
+
+template <bool kCount, bool kOne>
+__global__ void __launch_bounds__(kSortBlock)
+    bin_kernel(const BatchItemDev* __restrict__ items, const SortItemDev* __restrict__ sort, uint32_t n_items,
+               uint64_t total, uint32_t* __restrict__ hist, SortedRay* __restrict__ list,
+               unsigned long long* __restrict__ n_list, const OneItem one) {
+  __shared__ uint64_t s_begin[kMaxSharedItems];
+  if (!kOne) {
+    const uint32_t staged = n_items < kMaxSharedItems ? n_items : kMaxSharedItems;
+    for (uint32_t i = threadIdx.x; i < staged; i += blockDim.x) s_begin[i] = sort[i].begin;
+    __syncthreads();
+  }
+  // each warp bins kBinRays rays per round, its loads issued before any of them is binned
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * kBinRays;
+  for (uint64_t g0 = ((uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) * kBinRays; g0 < total; g0 += stride) {
+    float o[kBinRays][3], d[kBinRays][3];
+    uint64_t jj[kBinRays];
+    uint32_t at[kBinRays];
+#pragma unroll
+    for (uint32_t u = 0; u < kBinRays; ++u) {
+      const uint64_t g = g0 + 32 * u + lane;
+      at[u] = 0xFFFFFFFFu;  // no ray
+      jj[u] = 0;
+      if (g < total) {
+        if (kOne) {
+          const uint64_t j = g - one.sort.begin;
+          if (j < one.sort.n) {
+            at[u] = one.index;
+            jj[u] = j;
+          }
+        } else {
+          uint32_t lo = 0, hi = n_items - 1;  // the item: largest with begin <= g
+          while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            const uint64_t b = mid < kMaxSharedItems ? s_begin[mid] : sort[mid].begin;
+            if (b <= g)
+              lo = mid;
+            else
+              hi = mid - 1;
+          }
+          const uint64_t j = g - sort[lo].begin;  // an empty item shares its begin with the next one
+          if (j < sort[lo].n) {
+            at[u] = lo;
+            jj[u] = j;
+          }
+        }
+      }
+      if (at[u] != 0xFFFFFFFFu) {
+        const RaysView& rv = kOne ? one.rays : items[at[u]].rays;
+        const uint64_t j = jj[u];
+        o[u][0] = __ldg(rv.ox + j);
+        o[u][1] = __ldg(rv.oy + j);
+        o[u][2] = __ldg(rv.oz + j);
+        d[u][0] = __ldg(rv.dx + j);
+        d[u][1] = __ldg(rv.dy + j);
+        d[u][2] = __ldg(rv.dz + j);
+      }
+    }
+    bool enters[kBinRays];
+    SortedRay r[kBinRays];
+#pragma unroll
+    for (uint32_t u = 0; u < kBinRays; ++u) {
+      enters[u] = false;
+      if (at[u] != 0xFFFFFFFFu) {
+        if (kOne)
+          enters[u] = bin_ray<kCount>(one.scene, one.hits, one.sort, at[u], jj[u], o[u], d[u], r[u]);
+        else
+          enters[u] = bin_ray<kCount>(items[at[u]].scene, items[at[u]].hits, sort[at[u]], at[u], jj[u], o[u], d[u], r[u]);
+      }
+      if (enters[u]) atomicAdd(hist + r[u].bucket, 1u);  // a reduction: nothing waits for it
+    }
+    unsigned m[kBinRays];
+    uint32_t entering = 0;
+#pragma unroll
+    for (uint32_t u = 0; u < kBinRays; ++u) {
+      m[u] = __ballot_sync(0xFFFFFFFFu, enters[u]);
+      entering += __popc(m[u]);
+    }
+    if (entering == 0) continue;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(n_list, (unsigned long long)entering);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+#pragma unroll
+    for (uint32_t u = 0; u < kBinRays; ++u) {
+      if (enters[u]) {
+        float4* dst = reinterpret_cast<float4*>(list + base + __popc(m[u] & ((1u << lane) - 1u)));
+        const float4* src = reinterpret_cast<const float4*>(&r[u]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) dst[k] = src[k];
+      }
+      base += __popc(m[u]);
+    }
+  }
+}
+
+// Exclusive scan of the bucket counts in place, kScanTile counts per block.
+constexpr uint32_t kScanTile = 4096;
+constexpr uint32_t kScanPerThread = kScanTile / kSortBlock;  // 16
+
+// exclusive prefix of v over the block's threads; *block_sum gets the total
+__device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* warp_sums, uint32_t* block_sum) {
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t nw = blockDim.x >> 5;
+    uint32_t w = lane < nw ? warp_sums[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+      if (lane >= (uint32_t)o) w += y;
+    }
+    if (lane < nw) warp_sums[lane] = w;  // inclusive
+  }
+  __syncthreads();
+  const uint32_t before = warp ? warp_sums[warp - 1] : 0u;
+  *block_sum = warp_sums[(blockDim.x >> 5) - 1];
+  __syncthreads();  // warp_sums is reused by the next call
+  return before + x - v;
+}
+
+__global__ void __launch_bounds__(kSortBlock) scan_reduce(const uint32_t* __restrict__ hist, uint64_t nb,
+                                                          uint32_t* __restrict__ sums) {
+  __shared__ uint32_t warp_sums[32];
+  const uint64_t base = (uint64_t)blockIdx.x * kScanTile;
+  uint32_t v = 0;
+  for (uint32_t k = 0; k < kScanPerThread; ++k) {
+    const uint64_t b = base + k * kSortBlock + threadIdx.x;
+    if (b < nb) v += hist[b];
+  }
+  uint32_t total = 0;
+  block_exclusive(v, warp_sums, &total);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) scan_top(uint32_t* __restrict__ sums, uint32_t n) {
+  __shared__ uint32_t warp_sums[32];
+  uint32_t carry = 0;
+  for (uint32_t b0 = 0; b0 < n; b0 += blockDim.x) {
+    const uint32_t b = b0 + threadIdx.x;
+    const uint32_t v = b < n ? sums[b] : 0u;
+    uint32_t total = 0;
+    const uint32_t ex = block_exclusive(v, warp_sums, &total);
+    if (b < n) sums[b] = carry + ex;
+    carry += total;
+  }
+}
+
+__global__ void __launch_bounds__(kSortBlock) scan_down(uint32_t* __restrict__ hist, uint64_t nb,
+                                                        const uint32_t* __restrict__ sums) {
+  __shared__ uint32_t warp_sums[32];
+  __shared__ uint32_t tile[kScanTile];
+  const uint64_t base = (uint64_t)blockIdx.x * kScanTile;
+  for (uint32_t k = 0; k < kScanPerThread; ++k) {
+    const uint32_t t = k * kSortBlock + threadIdx.x;
+    tile[t] = base + t < nb ? hist[base + t] : 0u;
+  }
+  __syncthreads();
+  uint32_t v = 0;
+  for (uint32_t k = 0; k < kScanPerThread; ++k) v += tile[threadIdx.x * kScanPerThread + k];
+  uint32_t total = 0;
+  uint32_t run = sums[blockIdx.x] + block_exclusive(v, warp_sums, &total);
+  for (uint32_t k = 0; k < kScanPerThread; ++k) {
+    const uint32_t t = threadIdx.x * kScanPerThread + k;
+    const uint32_t c = tile[t];
+    tile[t] = run;
+    run += c;
+  }
+  __syncthreads();
+  for (uint32_t k = 0; k < kScanPerThread; ++k) {
+    const uint32_t t = k * kSortBlock + threadIdx.x;
+    if (base + t < nb) hist[base + t] = tile[t];
+  }
+}
+
+__global__ void __launch_bounds__(kSortBlock)
+    scatter_kernel(const SortedRay* __restrict__ list, const unsigned long long* __restrict__ n_list,
+                   uint32_t* __restrict__ offsets, SortedRay* __restrict__ sorted) {
+  const uint64_t n = *n_list;
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+    const float4* src = reinterpret_cast<const float4*>(list + k);
+    const float4 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2), d = __ldg(src + 3);
+    const uint32_t bucket = __float_as_uint(d.x);  // SortedRay::bucket
+    float4* dst = reinterpret_cast<float4*>(sorted + atomicAdd(offsets + bucket, 1u));
+    dst[0] = a;
+    dst[1] = b;
+    dst[2] = c;
+    dst[3] = d;
+  }
+}
+
+template <bool kCount, bool kOne>
+__global__ void __launch_bounds__(kBatchMaxBlock, 7)
+    sorted_cast_kernel(const BatchItemDev* __restrict__ items, const SortedRay* __restrict__ sorted,
+                       const unsigned long long* __restrict__ n_list, unsigned long long* __restrict__ counter,
+                       uint32_t chunk, const SceneView one_scene, const HitsView one_hits) {
+  __shared__ SharedLuts L;
+  fill_shared_luts(L);
+  __syncthreads();
+  const uint64_t n = *n_list;
+  const uint32_t lane = threadIdx.x & 31u;
+  for (;;) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(counter, (unsigned long long)chunk);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (base >= n) break;
+    for (uint32_t off = 0; off < chunk; off += 32) {
+      const uint64_t k = base + off + lane;
+      if (off + lane >= chunk || k >= n) continue;
+      const float4* src = reinterpret_cast<const float4*>(sorted + k);
+      const float4 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2), d = __ldg(src + 3);
+      const uint32_t target = __float_as_uint(c.y);
+      const uint64_t i = (uint64_t)__float_as_uint(d.z) | ((uint64_t)__float_as_uint(d.w) << 32);
+      const bool fast = (target >> 31) != 0u;
+      HitRecord h;
+      if (kOne) {
+        cast_entered<kCount>(one_scene, L, a.x, a.y, a.z, a.w, b.x, b.y, fast, b.z, b.w, c.x, target & 0x7FFFFFFFu, h);
+        write_hit(one_scene, one_hits, i, h);
+        if (kCount) write_counters(one_hits, i, h);
+      } else {
+        const BatchItemDev& it = items[__float_as_uint(c.z)];
+        cast_entered<kCount>(it.scene, L, a.x, a.y, a.z, a.w, b.x, b.y, fast, b.z, b.w, c.x, target & 0x7FFFFFFFu, h);
+        write_hit(it.scene, it.hits, i, h);
+        if (kCount) write_counters(it.hits, i, h);
+      }
+    }
+  }
+}
+
 }  // namespace svo
 
 // Workspace of the batched cast: device item table + work counter, and a
 // pinned host staging copy of the table.  Grows only when the item count grows.
 struct svo_batch_workspace {
   svo::BatchItemDev* d_items = nullptr;
-  unsigned long long* d_counter = nullptr;
-  svo::BatchItemDev* h_items = nullptr;  // pinned
-  cudaEvent_t copied = nullptr;           // the last table upload has left h_items
+  unsigned long long* d_counter = nullptr;  // [0] work counter, [1] length of the ray sort's list
+  svo::BatchItemDev* h_items = nullptr;     // pinned
+  svo::SortItemDev* d_sort = nullptr;       // the ray sort's item table
+  svo::SortItemDev* h_sort = nullptr;       // pinned
+  cudaEvent_t copied = nullptr;             // the last table upload has left h_items and h_sort
   uint32_t cap = 0;
   int sm_count = 0;
+  // ray sort buffers (sort_key 1), grown on demand
+  uint32_t* d_hist = nullptr;  // bucket counts, then bucket offsets
+  uint32_t* d_sums = nullptr;  // per scan tile
+  uint64_t hist_cap = 0;
+  svo::SortedRay* d_list = nullptr;    // entering rays as binned
+  svo::SortedRay* d_sorted = nullptr;  // entering rays in bucket order
+  uint64_t list_cap = 0;
 };
 
 using namespace svo;
@@ -208,7 +565,7 @@ svo_status svo_batch_workspace_create(svo_batch_workspace** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ws->sm_count, cudaDevAttrMultiProcessorCount, dev);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->d_counter, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&ws->d_counter, 2 * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws->copied, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     cudaFree(ws->d_counter);
@@ -225,6 +582,12 @@ void svo_batch_workspace_destroy(svo_batch_workspace* ws) {
   cudaFree(ws->d_items);
   cudaFree(ws->d_counter);
   cudaFreeHost(ws->h_items);
+  cudaFree(ws->d_sort);
+  cudaFreeHost(ws->h_sort);
+  cudaFree(ws->d_hist);
+  cudaFree(ws->d_sums);
+  cudaFree(ws->d_list);
+  cudaFree(ws->d_sorted);
   if (ws->copied) cudaEventDestroy(ws->copied);
   delete ws;
 }
@@ -243,20 +606,28 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
     SVO_CUDA_TRY(cudaStreamSynchronize(st));
     cudaFree(ws->d_items);
     cudaFreeHost(ws->h_items);
+    cudaFree(ws->d_sort);
+    cudaFreeHost(ws->h_sort);
     ws->d_items = nullptr;
     ws->h_items = nullptr;
+    ws->d_sort = nullptr;
+    ws->h_sort = nullptr;
     ws->cap = 0;
     const uint32_t cap = std::max<uint32_t>(n_items, 16);
     SVO_CUDA_TRY(cudaMalloc(&ws->d_items, cap * sizeof(BatchItemDev)));
     SVO_CUDA_TRY(cudaMallocHost(&ws->h_items, cap * sizeof(BatchItemDev)));
+    SVO_CUDA_TRY(cudaMalloc(&ws->d_sort, cap * sizeof(SortItemDev)));
+    SVO_CUDA_TRY(cudaMallocHost(&ws->h_sort, cap * sizeof(SortItemDev)));
     ws->cap = cap;
   } else if (!in_capture) {
-    // the pinned staging table is reused: wait until its previous upload has left it
+    // the pinned staging tables are reused: wait until their previous upload has left them
     SVO_CUDA_TRY(cudaEventSynchronize(ws->copied));
   }
   const uint32_t shape = (cfg && cfg->block_shape) ? cfg->block_shape : 3;
   if (shape < 3 || shape > 5) return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: block_shape must be 0, 3, 4 or 5");
-  uint64_t total = 0;
+  const uint32_t sort_key = cfg ? cfg->sort_key : 0;
+  if (sort_key > 1) return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: sort_key must be 0 or 1");
+  uint64_t total = 0, sort_total = 0, buckets = 0;
   bool count = false;
   for (uint32_t i = 0; i < n_items; ++i) {
     const svo_batch_item& it = items[i];
@@ -264,14 +635,100 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
     if (!it.scene->dev.valid) return fail(SVO_ERR_NOT_UPLOADED, "svo_cast_batched: scene not uploaded");
     if (it.n && (!it.rays.ox || !it.rays.oy || !it.rays.oz || !it.rays.dx || !it.rays.dy || !it.rays.dz))
       return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: NULL ray array");
-    total += item_dev(it, total, shape, ws->h_items[i]);
+    const bool sorted = sort_key == 1 && it.row_length == 0 && it.n > 0;
+    total += item_dev(it, total, shape, ws->h_items[i], !sorted);
+    SortItemDev& si = ws->h_sort[i];
+    si.begin = sort_total;
+    si.n = sorted ? it.n : 0;
+    si.bits = sorted ? sort_bits(it.n) : 0;
+    si.bucket_base = (uint32_t)buckets;
+    if (sorted) {
+      sort_total += it.n;
+      buckets += 8ull << (3 * si.bits);
+    }
     count |= counts_requested(it.hits);
   }
-  if (total == 0) return SVO_OK;
+  if (total == 0 && sort_total == 0) return SVO_OK;
+  if (sort_total >= (1ull << 32) || buckets >= (1ull << 32))
+    return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: the ray sort takes fewer than 2^32 rays per call");
   const uint32_t block = (cfg && cfg->block) ? cfg->block : 128;
   const uint32_t chunk = (cfg && cfg->rays_per_chunk) ? cfg->rays_per_chunk : 64;
   if (block % 32 != 0 || block > kBatchMaxBlock || chunk == 0)
     return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: block must be a multiple of 32 and at most 128");
+  if (sort_total > ws->list_cap || buckets > ws->hist_cap) {
+    if (in_capture)
+      return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: the ray sort's buffers must be sized before stream capture");
+    SVO_CUDA_TRY(cudaStreamSynchronize(st));
+    if (sort_total > ws->list_cap) {
+      cudaFree(ws->d_list);
+      cudaFree(ws->d_sorted);
+      ws->d_list = ws->d_sorted = nullptr;
+      ws->list_cap = 0;
+      SVO_CUDA_TRY(cudaMalloc(&ws->d_list, sort_total * sizeof(SortedRay)));
+      SVO_CUDA_TRY(cudaMalloc(&ws->d_sorted, sort_total * sizeof(SortedRay)));
+      ws->list_cap = sort_total;
+    }
+    if (buckets > ws->hist_cap) {
+      cudaFree(ws->d_hist);
+      cudaFree(ws->d_sums);
+      ws->d_hist = ws->d_sums = nullptr;
+      ws->hist_cap = 0;
+      SVO_CUDA_TRY(cudaMalloc(&ws->d_hist, buckets * sizeof(uint32_t)));
+      SVO_CUDA_TRY(cudaMalloc(&ws->d_sums, (buckets / kScanTile + 1) * sizeof(uint32_t)));
+      ws->hist_cap = buckets;
+    }
+  }
+  SVO_CUDA_TRY(cudaMemcpyAsync(ws->d_items, ws->h_items, n_items * sizeof(BatchItemDev), cudaMemcpyHostToDevice, st));
+  if (sort_total)
+    SVO_CUDA_TRY(cudaMemcpyAsync(ws->d_sort, ws->h_sort, n_items * sizeof(SortItemDev), cudaMemcpyHostToDevice, st));
+  if (!in_capture) SVO_CUDA_TRY(cudaEventRecord(ws->copied, st));
+  if (sort_total) {
+    unsigned long long* n_list = ws->d_counter + 1;
+    SVO_CUDA_TRY(cudaMemsetAsync(ws->d_counter, 0, 2 * sizeof(unsigned long long), st));
+    SVO_CUDA_TRY(cudaMemsetAsync(ws->d_hist, 0, buckets * sizeof(uint32_t), st));
+    // a single sorted item rides in the kernel parameters
+    uint32_t n_sorted = 0;
+    OneItem one{};
+    for (uint32_t i = 0; i < n_items; ++i)
+      if (ws->h_sort[i].n) {
+        if (n_sorted++ == 0) {
+          one.scene = ws->h_items[i].scene;
+          one.rays = ws->h_items[i].rays;
+          one.hits = ws->h_items[i].hits;
+          one.sort = ws->h_sort[i];
+          one.index = i;
+        }
+      }
+    const bool single = n_sorted == 1;
+    int bin_per_sm = 0;
+    SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &bin_per_sm, single ? (count ? bin_kernel<true, true> : bin_kernel<false, true>)
+                            : (count ? bin_kernel<true, false> : bin_kernel<false, false>),
+        kSortBlock, 0));
+    const uint64_t fill = (uint64_t)ws->sm_count * (uint64_t)std::max(bin_per_sm, 1);
+    const unsigned bin_grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(fill, (sort_total + kSortBlock - 1) / kSortBlock));
+    auto bin = single ? (count ? bin_kernel<true, true> : bin_kernel<false, true>)
+                      : (count ? bin_kernel<true, false> : bin_kernel<false, false>);
+    bin<<<bin_grid, kSortBlock, 0, st>>>(ws->d_items, ws->d_sort, n_items, sort_total, ws->d_hist, ws->d_list, n_list, one);
+    const uint32_t tiles = (uint32_t)((buckets + kScanTile - 1) / kScanTile);
+    scan_reduce<<<tiles, kSortBlock, 0, st>>>(ws->d_hist, buckets, ws->d_sums);
+    scan_top<<<1, 1024, 0, st>>>(ws->d_sums, tiles);
+    scan_down<<<tiles, kSortBlock, 0, st>>>(ws->d_hist, buckets, ws->d_sums);
+    scatter_kernel<<<bin_grid, kSortBlock, 0, st>>>(ws->d_list, n_list, ws->d_hist, ws->d_sorted);
+    auto cast = single ? (count ? sorted_cast_kernel<true, true> : sorted_cast_kernel<false, true>)
+                       : (count ? sorted_cast_kernel<true, false> : sorted_cast_kernel<false, false>);
+    int per_sm = (cfg && cfg->blocks_per_sm) ? (int)cfg->blocks_per_sm : 0;
+    if (per_sm == 0) {
+      SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cast, block, 0));
+      per_sm = std::max(per_sm, 1);
+    }
+    const uint64_t warps_needed = (sort_total + chunk - 1) / chunk;
+    uint64_t grid = (uint64_t)ws->sm_count * (uint64_t)per_sm;
+    grid = std::max<uint64_t>(1, std::min<uint64_t>(grid, (warps_needed * 32 + block - 1) / block));
+    cast<<<(unsigned)grid, block, 0, st>>>(ws->d_items, ws->d_sorted, n_list, ws->d_counter, chunk, one.scene, one.hits);
+    SVO_CUDA_TRY(cudaGetLastError());
+  }
+  if (total == 0) return SVO_OK;
   int per_sm = (cfg && cfg->blocks_per_sm) ? (int)cfg->blocks_per_sm : 0;
   if (per_sm == 0) {
     if (count)
@@ -284,8 +741,6 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
   uint64_t grid = (uint64_t)ws->sm_count * (uint64_t)per_sm;
   grid = std::min<uint64_t>(grid, (warps_needed * 32 + block - 1) / block);
   grid = std::max<uint64_t>(grid, 1);
-  SVO_CUDA_TRY(cudaMemcpyAsync(ws->d_items, ws->h_items, n_items * sizeof(BatchItemDev), cudaMemcpyHostToDevice, st));
-  if (!in_capture) SVO_CUDA_TRY(cudaEventRecord(ws->copied, st));
   SVO_CUDA_TRY(cudaMemsetAsync(ws->d_counter, 0, sizeof(unsigned long long), st));
   if (count)
     batched_kernel<true><<<(unsigned)grid, block, 0, st>>>(ws->d_items, n_items, total, ws->d_counter, chunk);
@@ -357,6 +812,8 @@ svo_status svo_cast_batched_noalloc(const svo_batch_item* items, uint32_t n_item
   const uint32_t shape = (cfg && cfg->block_shape) ? cfg->block_shape : 3;
   if (shape < 3 || shape > 5)
     return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: block_shape must be 0, 3, 4 or 5");
+  if (cfg && cfg->sort_key)
+    return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: the ray sort (sort_key) needs a batch workspace");
   uint64_t total = 0;
   bool count = false;
   for (uint32_t i = 0; i < n_items; ++i) {
