@@ -44,17 +44,18 @@ uint64_t item_dev(const svo_batch_item& it, uint64_t begin, uint32_t shape, Batc
   return 32 * d.order.claims;
 }
 
-constexpr uint32_t kMaxSharedItems = 1024;  // prefix sums staged in shared memory
+constexpr uint32_t kMaxSharedItems = 256;  // prefix sums staged in shared memory (the rest read from the table)
 
 // At most kBatchMaxBlock threads per block with 7 resident blocks per SM (72 registers, a few
 // spilled bytes); the launch configuration is checked against the block limit.
 constexpr uint32_t kBatchMaxBlock = 128;
 
 // Rays that miss their octree's root box get their miss written at once; the entering rays of a
-// partly entering round of 32 indices wait in the warp's slice of shared memory (with the point where
-// they enter and their item) until 32 of them fill the warp.
+// partly entering round of 32 indices wait in the warp's slice of shared memory (their index, item,
+// the point where they enter and its octant) until 32 of them fill the warp; their origin and
+// direction are read again when they are cast (less shared memory per block leaves more L1).
 struct WaitingBatchRays {
-  float o[3][64], d[3][64], p[3][64];
+  float p[3][64];
   uint32_t target[64];  // octant of the entry point; bit 31: fast form
   uint32_t item[64];
   unsigned long long i[64];
@@ -78,7 +79,7 @@ __global__ void __launch_bounds__(kBatchMaxBlock, 7)
   unsigned long long base = 0;        // the warp's chunk
   uint32_t next = chunk;              // offset of the next round of 32 indices in it
   for (;;) {
-    bool have = false, fast = false;
+    bool have = false, fast = false, waited = false;
     uint64_t i = 0;
     uint32_t item = 0, target = 0;
     float ox = 0.0f, oy = 0.0f, oz = 0.0f, dx = 0.0f, dy = 0.0f, dz = 0.0f, px = 0.0f, py = 0.0f, pz = 0.0f;
@@ -139,12 +140,6 @@ __global__ void __launch_bounds__(kBatchMaxBlock, 7)
       }
       if (enters) {
         const uint32_t k = count + __popc(m & ((1u << lane) - 1u));
-        w.o[0][k] = ox;
-        w.o[1][k] = oy;
-        w.o[2][k] = oz;
-        w.d[0][k] = dx;
-        w.d[1][k] = dy;
-        w.d[2][k] = dz;
         w.p[0][k] = px;
         w.p[1][k] = py;
         w.p[2][k] = pz;
@@ -160,12 +155,6 @@ __global__ void __launch_bounds__(kBatchMaxBlock, 7)
       const uint32_t take = count < 32 ? count : 32;
       if (lane < take) {
         const uint32_t k = count - take + lane;
-        ox = w.o[0][k];
-        oy = w.o[1][k];
-        oz = w.o[2][k];
-        dx = w.d[0][k];
-        dy = w.d[1][k];
-        dz = w.d[2][k];
         px = w.p[0][k];
         py = w.p[1][k];
         pz = w.p[2][k];
@@ -174,12 +163,22 @@ __global__ void __launch_bounds__(kBatchMaxBlock, 7)
         item = w.item[k];
         i = w.i[k];
         have = true;
+        waited = true;
       }
       count -= take;
       __syncwarp();
     }
     if (!have) continue;
     const BatchItemDev& it = items[item];
+    if (waited) {  // origin and direction again from the item's arrays
+      const RaysView& r = it.rays;
+      ox = __ldg(r.ox + i);
+      oy = __ldg(r.oy + i);
+      oz = __ldg(r.oz + i);
+      dx = __ldg(r.dx + i);
+      dy = __ldg(r.dy + i);
+      dz = __ldg(r.dz + i);
+    }
     HitRecord h;
     cast_entered<kCount>(it.scene, L, ox, oy, oz, dx, dy, dz, fast, px, py, pz, target, h);
     write_hit(it.scene, it.hits, i, h);
