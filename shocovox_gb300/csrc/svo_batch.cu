@@ -213,17 +213,15 @@ struct __align__(16) SortedRay {
   float o[3], d[3], p[3];
   uint32_t target;  // octant of the entry point; bit 31: fast form
   uint32_t item;
-  uint32_t rank;    // (unused)
-  uint32_t bucket;  // (unsorted list)
-  uint32_t pad;
+  uint32_t bucket;
+  uint32_t pad[2];
   unsigned long long i;  // ray index in the item
 };
 static_assert(sizeof(SortedRay) == 64, "SortedRay is four 16-byte pieces");
 // the kernels read a SortedRay as four float4 (a, b, c, d): o = a.xyz, d = (a.w, b.x, b.y),
-// p = (b.z, b.w, c.x), target = c.y, item = c.z, rank = c.w, bucket = d.x, i = d.zw
+// p = (b.z, b.w, c.x), target = c.y, item = c.z, bucket = c.w, i = d.zw
 static_assert(offsetof(SortedRay, d) == 12 && offsetof(SortedRay, p) == 24 && offsetof(SortedRay, target) == 36 &&
-                  offsetof(SortedRay, item) == 40 && offsetof(SortedRay, rank) == 44 &&
-                  offsetof(SortedRay, bucket) == 48 && offsetof(SortedRay, i) == 56,
+                  offsetof(SortedRay, item) == 40 && offsetof(SortedRay, bucket) == 44 && offsetof(SortedRay, i) == 56,
               "SortedRay layout");
 
 // bits of the entry point's Morton code per axis for an item of n rays: about 16 rays a bucket
@@ -253,7 +251,8 @@ struct OneItem {
   uint32_t index;
 };
 
-// Ray j of an item (origin o, direction d): its miss written at once, or its record (with its
+// Ray j of an item (origin o, direction d): its miss written at once (a miss is written for an
+// entering ray too, until the cast overwrites it), and for an entering ray its record (with its
 // bucket) in r.
 template <bool kCount>
 __device__ __forceinline__ bool bin_ray(const SceneView& sc, const HitsView& hv, const SortItemDev& si,
@@ -263,13 +262,14 @@ __device__ __forceinline__ bool bin_ray(const SceneView& sc, const HitsView& hv,
   const bool fast = !sc.literal && !isnan(dx) && !isnan(dy) && !isnan(dz);
   float px = ox, py = oy, pz = oz;
   uint32_t target = 0;
-  if (fast && !fast_entry(sc, ox, oy, oz, dx, dy, dz, px, py, pz, target)) {
-    HitRecord h;
-    miss_record(h);
-    write_hit(sc, hv, j, h);
-    if (kCount) write_counters(hv, j, h);
-    return false;
-  }
+  const bool enters = !fast || fast_entry(sc, ox, oy, oz, dx, dy, dz, px, py, pz, target);
+  // every lane writes a miss, the entering rays' ones to be overwritten by the cast: whole sectors of
+  // the hit arrays are written at once instead of sectors with holes that DRAM must read back
+  HitRecord h;
+  miss_record(h);
+  write_hit(sc, hv, j, h);
+  if (kCount) write_counters(hv, j, h);
+  if (!enters) return false;
   // the key: only an order, so any rounding will do (a literal ray keys on its origin)
   const uint32_t q = 1u << si.bits;
   const float scale = (float)q * sc.inv_size;
@@ -289,8 +289,7 @@ __device__ __forceinline__ bool bin_ray(const SceneView& sc, const HitsView& hv,
   r.target = target | (fast ? 0x80000000u : 0u);
   r.item = item;
   r.bucket = si.bucket_base + (oct << (3 * si.bits)) + (spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2));
-  r.rank = 0;
-  r.pad = 0;
+  r.pad[0] = r.pad[1] = 0;
   r.i = j;
   return true;
 }
@@ -485,7 +484,7 @@ __global__ void __launch_bounds__(kSortBlock)
   for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
     const float4* src = reinterpret_cast<const float4*>(list + k);
     const float4 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2), d = __ldg(src + 3);
-    const uint32_t bucket = __float_as_uint(d.x);  // SortedRay::bucket
+    const uint32_t bucket = __float_as_uint(c.w);  // SortedRay::bucket
     float4* dst = reinterpret_cast<float4*>(sorted + atomicAdd(offsets + bucket, 1u));
     dst[0] = a;
     dst[1] = b;
@@ -677,28 +676,30 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
       ws->hist_cap = buckets;
     }
   }
-  SVO_CUDA_TRY(cudaMemcpyAsync(ws->d_items, ws->h_items, n_items * sizeof(BatchItemDev), cudaMemcpyHostToDevice, st));
-  if (sort_total)
+  // a single sorted item rides in the kernel parameters
+  uint32_t n_sorted = 0;
+  OneItem one{};
+  for (uint32_t i = 0; i < n_items; ++i)
+    if (ws->h_sort[i].n) {
+      if (n_sorted++ == 0) {
+        one.scene = ws->h_items[i].scene;
+        one.rays = ws->h_items[i].rays;
+        one.hits = ws->h_items[i].hits;
+        one.sort = ws->h_sort[i];
+        one.index = i;
+      }
+    }
+  const bool single = n_sorted == 1;
+  // the tables are read by the claim-order kernel and by the sort's kernels of several items
+  if (total > 0 || (sort_total > 0 && !single))
+    SVO_CUDA_TRY(cudaMemcpyAsync(ws->d_items, ws->h_items, n_items * sizeof(BatchItemDev), cudaMemcpyHostToDevice, st));
+  if (sort_total > 0 && !single)
     SVO_CUDA_TRY(cudaMemcpyAsync(ws->d_sort, ws->h_sort, n_items * sizeof(SortItemDev), cudaMemcpyHostToDevice, st));
   if (!in_capture) SVO_CUDA_TRY(cudaEventRecord(ws->copied, st));
   if (sort_total) {
     unsigned long long* n_list = ws->d_counter + 1;
     SVO_CUDA_TRY(cudaMemsetAsync(ws->d_counter, 0, 2 * sizeof(unsigned long long), st));
     SVO_CUDA_TRY(cudaMemsetAsync(ws->d_hist, 0, buckets * sizeof(uint32_t), st));
-    // a single sorted item rides in the kernel parameters
-    uint32_t n_sorted = 0;
-    OneItem one{};
-    for (uint32_t i = 0; i < n_items; ++i)
-      if (ws->h_sort[i].n) {
-        if (n_sorted++ == 0) {
-          one.scene = ws->h_items[i].scene;
-          one.rays = ws->h_items[i].rays;
-          one.hits = ws->h_items[i].hits;
-          one.sort = ws->h_sort[i];
-          one.index = i;
-        }
-      }
-    const bool single = n_sorted == 1;
     int bin_per_sm = 0;
     SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &bin_per_sm, single ? (count ? bin_kernel<true, true> : bin_kernel<false, true>)
