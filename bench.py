@@ -7,14 +7,25 @@ terrain with caves (3D noise threshold 0.55, ~9.4% occupancy), 4 pinhole
 cameras at 1920x1080 and 70 deg FOV at seeded positions above the terrain:
 8,294,400 f32 rays per step.  A step is one cast of the whole batch.
 
-  value  rays/s with rays and hits resident in HBM (device pointers, svo_cast)
-  e2e    the same batch through the host-buffer C-ABI call svo_cast_host:
-         host->device copy of the rays and device->host copy of the results
-         inside the timed region
+  value   rays/s with rays and hits resident in HBM (device pointers, svo_cast_rows)
+  e2e     the same batch through the host-buffer C-ABI call svo_cast_host_rows:
+          host->device copy of the rays and device->host copy of the results
+          inside the timed region
+  parity  every ray of the batch cast again by the CPU oracle (a restatement of
+          the reference's get_by_ray) and compared field by field with the
+          timed launch, the instrumented launch, the other ray orders and the
+          host-buffer path: hit identity and counters exactly, impact point and
+          normal within 1e-4 voxel units.  A mismatch makes the run exit 1.
 
-`--impl reference` times the oracle's CPU cast (a restatement of the
-reference's get_by_ray; the Rust crate cannot be built here) on the host
-cores over a bounded sample of the same rays.
+The default run also measures, in sub-objects of its one JSON line
+("north_star"), the plain cast against the batched and served forms on the
+incoherent-ray, multi-scene and served workloads, each over repeated timings
+with its own parity check and clock record.
+
+`--impl reference` times the oracle's CPU cast (the reference is a Rust crate
+that cannot be built here) on all host cores over the whole batch of the same
+workload, with the scene and rays made by the oracle's own generators: it
+loads no product code.
 """
 import argparse
 import json
@@ -39,7 +50,9 @@ WORKLOADS = {
     "incoherent1024": dict(kind=2, size=1024, brick_dim=8, seed=0x5EED0003, occupancy=0.05,
                            rays=("sphere", 1 << 22)),
     "multiscene64": dict(multi=64, seed=0x5EED0004),
-    "served16": dict(served=16, seed=0x5EED0005, rate=2000.0, requests=600, budget_gb=60.0),
+    # 10,000 Poisson requests at 2,000/s (5 s); the device budget is half the 16 scene images, so
+    # scenes are evicted and uploaded again while requests run
+    "served16": dict(served=16, seed=0x5EED0005, rate=2000.0, requests=10000, budget_frac=0.5, repeats=3),
     # terrain512 with MIP maps, cast through get_by_ray_at_lod at a viewing distance of 256
     "lod512": dict(lod=256.0, kind=1, size=512, brick_dim=8, seed=0x5EED0002, spheres=0, octaves=3,
                    base_freq=1.0 / 128, height_lo=0.02 * S_TERRAIN, height_hi=0.33 * S_TERRAIN, cave_threshold=0.55,
@@ -54,16 +67,92 @@ OUT_FIELDS = ("status", "entry_kind", "albedo", "user", "px", "py", "pz", "nx", 
 COUNTERS = ("node_visits", "child_reads", "voxel_reads", "run_visits")
 OUT_BYTES = {"status": 1, "entry_kind": 1, "albedo": 4, "user": 4, "px": 4, "py": 4, "pz": 4, "nx": 4, "ny": 4,
              "nz": 4}
+RAY_KEYS = ("ox", "oy", "oz", "dx", "dy", "dz")
+REPEATS = 5  # timed repeats of each spec variant (median and spread are reported)
+
+# ---- parity against the oracle --------------------------------------------------------------------
+TOL = 1e-4  # voxel units: impact point and normal
+ID_FIELDS = ("status", "brick_octant", "entry_kind", "node_key", "voxel_index", "pix", "albedo", "user")
+FLOAT_FIELDS = ("px", "py", "pz", "nx", "ny", "nz")
+CHECKED_COUNTERS = ("node_visits", "child_reads", "voxel_reads")
+ALL_CHECKED = ID_FIELDS + FLOAT_FIELDS + CHECKED_COUNTERS
 
 
-def scene_ops(svo, w):
-    return svo.gen_scene(w["kind"], w["size"], w["brick_dim"], w["seed"], occupancy=w.get("occupancy", 0.1),
+def compare_hits(got, ref, label=""):
+    """Compares product results `got` (host arrays) with the oracle's cast `ref` of the same rays, over
+    the fields `got` has: hit identity and counters exactly, point and normal within TOL (NaN on both
+    sides agrees).  Returns a parity record."""
+    fields = [k for k in ALL_CHECKED if k in got]
+    n = len(got[fields[0]]) if fields else 0
+    bad = np.zeros(n, dtype=bool)
+    err = {"p": 0.0, "n": 0.0}
+    first = {}
+    for k in fields:
+        a, b = np.asarray(got[k]), np.asarray(ref[k])
+        if k in FLOAT_FIELDS:
+            a64, b64 = a.astype(np.float64), b.astype(np.float64)
+            same = (a64 == b64) | (np.isnan(a64) & np.isnan(b64))
+            with np.errstate(invalid="ignore"):
+                d = np.where(same, 0.0, np.abs(a64 - b64))
+            d = np.where(np.isnan(d), np.inf, d)
+            off = ~(d <= TOL)
+            if n:
+                err[k[0]] = max(err[k[0]], float(d.max()))
+        else:
+            off = a.astype(np.uint32) != b.astype(np.uint32)
+        if off.any():
+            first[k] = int(np.argmax(off))
+        bad |= off
+    rec = {"rays_checked": n, "mismatches": int(bad.sum()), "fields": fields,
+           "max_point_err": _finite(err["p"]), "max_normal_err": _finite(err["n"]), "tolerance": TOL}
+    if first:
+        rec["first_mismatch"] = {k: int(v) for k, v in first.items()}
+    if label:
+        rec["what"] = label
+    return rec
+
+
+def _finite(v):
+    return v if np.isfinite(v) else "inf"
+
+
+def merge_parity(recs):
+    """One record over several checks: rays and mismatches add up, the largest errors are kept."""
+    recs = [r for r in recs if r]
+    if not recs:
+        return None
+
+    def mx(k):
+        vals = [r[k] for r in recs]
+        return "inf" if "inf" in vals else max(vals)
+    return {"rays_checked": sum(r["rays_checked"] for r in recs), "mismatches": sum(r["mismatches"] for r in recs),
+            "checks": [r.get("what", "") for r in recs], "max_point_err": mx("max_point_err"),
+            "max_normal_err": mx("max_normal_err"), "tolerance": TOL,
+            "bad": [r for r in recs if r["mismatches"]][:4]}
+
+
+def parity_failed(rec):
+    """True when a record or any nested record reports a mismatch (or an unchecked error)."""
+    if isinstance(rec, dict):
+        if "parity" in rec and isinstance(rec["parity"], dict) and rec["parity"].get("mismatches", 0):
+            return True
+        if rec.get("error"):
+            return True
+        return any(parity_failed(v) for k, v in rec.items() if k != "parity")
+    if isinstance(rec, list):
+        return any(parity_failed(v) for v in rec)
+    return False
+
+
+# ---- workload generation (gen = the product module or the oracle module: same signatures) -------
+def scene_ops(gen, w):
+    return gen.gen_scene(w["kind"], w["size"], w["brick_dim"], w["seed"], occupancy=w.get("occupancy", 0.1),
                          spheres=w.get("spheres", 0), octaves=w.get("octaves", 2), base_freq=w.get("base_freq", 1 / 32),
                          height_lo=w.get("height_lo", 0.0), height_hi=w.get("height_hi", 0.0),
                          cave_threshold=w.get("cave_threshold", 0.55))
 
 
-def make_rays(svo, w):
+def make_rays(gen, w):
     spec = w["rays"]
     S = float(w["size"])
     rng = np.random.default_rng(w["seed"])
@@ -73,7 +162,7 @@ def make_rays(svo, w):
         for _ in range(ncam):
             eye = [rng.uniform(0.15, 0.85) * S, 0.45 * S, rng.uniform(0.15, 0.85) * S]
             target = [rng.uniform(0.1, 0.9) * S, 0.1 * S, rng.uniform(0.1, 0.9) * S]
-            o, d = svo.gen_camera_rays(eye, target, fov, width, height)
+            o, d = gen.gen_camera_rays(eye, target, fov, width, height)
             os_.append(o)
             ds.append(d)
         return np.concatenate(os_), np.concatenate(ds)
@@ -82,9 +171,9 @@ def make_rays(svo, w):
         az, el = rng.uniform(0, 2 * np.pi), 0.5
         c = S / 2
         eye = [c + 200 * np.cos(el) * np.sin(az), c + 200 * np.sin(el), c + 200 * np.cos(el) * np.cos(az)]
-        return svo.gen_camera_rays(eye, [c, c, c], fov, width, height)
+        return gen.gen_camera_rays(eye, [c, c, c], fov, width, height)
     if spec[0] == "sphere":
-        return svo.gen_sphere_rays([S / 2] * 3, S * np.sqrt(3.0) / 2, spec[1], w["seed"])
+        return gen.gen_sphere_rays([S / 2] * 3, S * np.sqrt(3.0) / 2, spec[1], w["seed"])
     raise ValueError(spec)
 
 
@@ -132,6 +221,7 @@ class ClockSampler:
             threading.Thread(target=self._read, daemon=True).start()
         except (OSError, ValueError):
             self.proc = None
+        return self
 
     def _read(self):
         for line in self.proc.stdout:
@@ -199,34 +289,62 @@ def oracle_tree_async(ops, w):
     return th, box
 
 
-def cpu_cast_rate(tree, origins, dirs, target_s, threads, **cast_args):
-    """Rays/s of the oracle cast over a strided sample sized for about target_s seconds."""
-    n = len(origins)
-    probe = max(1, n // 20000)
-    t0 = time.perf_counter()
-    tree.cast(origins[::probe], dirs[::probe], threads=threads, **cast_args)
-    rate = len(origins[::probe]) / max(time.perf_counter() - t0, 1e-6)
-    m = int(min(n, max(20000, rate * target_s)))
-    step = max(1, n // m)
-    so, sd = origins[::step], dirs[::step]
-    t0 = time.perf_counter()
-    tree.cast(so, sd, threads=threads, **cast_args)
-    dt = time.perf_counter() - t0
-    reps = 1
-    # a whole batch that takes the CPU less than the target is cast again until the target is reached
-    if step == 1 and dt < target_s:
-        more = int(min(1000, target_s / max(dt, 1e-6)))
-        t0 = time.perf_counter()
-        for _ in range(more):
-            tree.cast(so, sd, threads=threads, **cast_args)
-        dt, reps = time.perf_counter() - t0, more
-    return reps * len(so) / dt, reps * len(so), step, dt
+def host_fields(svo, d):
+    """Device result tensors -> host numpy arrays of the product's field types."""
+    return {k: v.cpu().numpy().view(svo.HIT_FIELDS[k]) for k, v in d.items()}
 
 
-def batched_variants(svo, torch, scene, rp, hp, n, stream, args, row=0):
-    """The persistent work-queue kernel on the same batch: a short autotune sweep, then K timed steps."""
-    ws = svo.BatchWorkspace()
-    items = [(scene, rp, n, hp, row)]
+def device_outputs(torch, svo, n, dev, fields):
+    tmap = {np.uint8: torch.uint8, np.uint32: torch.int32, np.float32: torch.float32}
+    return {k: torch.empty(max(n, 1), dtype=tmap[svo.HIT_FIELDS[k]], device=dev) for k in fields}
+
+
+def spread(n_rays, ms_list):
+    """Median Mrays/s over repeats with the slowest and fastest repeat."""
+    ms = np.asarray(ms_list, dtype=np.float64)
+    rate = n_rays / (ms / 1e3) / 1e6
+    return {"value": round(float(np.median(rate)), 3), "min": round(float(rate.min()), 3),
+            "max": round(float(rate.max()), 3), "ms_per_step": round(float(np.median(ms)), 4),
+            "repeats": len(ms_list)}
+
+
+def versus(batched, plain):
+    """How a batched form compares with the plain cast over repeats: median ratio, and whether its
+    slowest repeat still beats plain's fastest (a win outside the run-to-run spread)."""
+    return {"median_ratio": round(batched["value"] / plain["value"], 4),
+            "beats_plain": batched["value"] > plain["value"],
+            "beats_plain_outside_spread": batched["min"] > plain["max"]}
+
+
+def interleaved_repeats(variants, steps, repeats, stream, torch):
+    """Times every variant (name -> fn) over `steps` calls, `repeats` times, interleaving the variants so
+    that drift of the clocks affects all alike.  Returns name -> [ms per step]."""
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {k: [] for k in variants}
+    for _ in range(repeats):
+        for k, fn in variants.items():
+            fn()
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(steps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            out[k].append(e0.elapsed_time(e1) / steps)
+    return out
+
+
+def batched_launches(items, sort_key):
+    """Kernel launches of one svo_cast_batched call: the claim-order cast if any item is cast in claim
+    order, plus the ray sort's bin, three scan, scatter and cast launches if any item is sorted."""
+    sorted_items = [it for it in items if sort_key and not (len(it) > 4 and it[4]) and it[2]]
+    claimed = [it for it in items if it[2] and it not in sorted_items]
+    return (1 if claimed else 0) + (6 if sorted_items else 0)
+
+
+def sweep_batched(svo, torch, ws, items, stream, rows):
+    """Short autotune sweep of the batched cast on `items`: threads per block x rays per claim x ray-block
+    shape (items with a row length) or ray-sort key (items without).  Returns [(cfg tuple, ms)]."""
     s = stream.cuda_stream
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
@@ -243,35 +361,274 @@ def batched_variants(svo, torch, scene, rp, hp, n, stream, args, row=0):
     sweep = []
     for block in (64, 96, 128):
         for chunk in (32, 64, 256):
-            for shape in ((3, 4) if row else (0,)):
-                for sort in ((0,) if row else (0, 1)):
-                    cfg = svo.LaunchConfig(block, chunk, 0, shape, sort)
-                    sweep.append(((block, chunk, shape, sort), timed(cfg, 2)))
-    (block, chunk, shape, sort), _ = min(sweep, key=lambda t: t[1])
-    ms = timed(svo.LaunchConfig(block, chunk, 0, shape, sort), args.steps)
-    out = {"persistent_autotuned": {"value": round(n / (ms / 1e3) / 1e6, 3), "unit": "Mrays/s",
-                                    "ms_per_step": round(ms, 4), "block": block, "rays_per_chunk": chunk,
-                                    "block_shape": shape, "sort_key": sort,
-                                    "launches_per_step": batched_launches(items, sort)},
-           "sweep_ms": {"%dx%dx%dx%d" % k: round(v, 3) for k, v in sweep}}
-    if not row:
-        # the best of each ray order, timed over K steps
-        for so in (0, 1):
-            (b, c, sh, _), _ = min((t for t in sweep if t[0][3] == so), key=lambda t: t[1])
-            ms = timed(svo.LaunchConfig(b, c, 0, sh, so), args.steps)
-            out["persistent_sort%d" % so] = {"value": round(n / (ms / 1e3) / 1e6, 3), "unit": "Mrays/s",
-                                             "ms_per_step": round(ms, 4), "block": b, "rays_per_chunk": c}
-    return out
+            for shape in ((3, 4) if rows else (0,)):
+                for sort in ((0,) if rows else (0, 1)):
+                    sweep.append(((block, chunk, shape, sort), timed(svo.LaunchConfig(block, chunk, 0, shape, sort), 2)))
+    return sweep
 
 
-def batched_launches(items, sort_key):
-    """Kernel launches of one svo_cast_batched call: the claim-order cast if any item is cast in claim
-    order, plus the ray sort's bin, three scan, scatter and cast launches if any item is sorted."""
-    sorted_items = [it for it in items if sort_key and not (len(it) > 4 and it[4]) and it[2]]
-    claimed = [it for it in items if it[2] and it not in sorted_items]
-    return (1 if claimed else 0) + (6 if sorted_items else 0)
+# ---- single scene: terrain512 (default), heightfield128, incoherent1024 ----------------------------
+def run_single(args, w, workload):
+    """The plain cast of one scene's batch (svo_cast_rows for camera images), with the ray orders, the
+    persistent batched kernel and the host-buffer path beside it, every output checked against the
+    oracle's cast of the whole batch."""
+    rank, local_rank, world = dist_env()
+    import torch
+    import shocovox_gb300 as svo
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")  # timing reduction only; the cast itself has no collective
+        pg = dist
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+
+    t0 = time.perf_counter()
+    ops = scene_ops(svo, w)
+    want_check = rank == 0 and not args.no_parity
+    if want_check:
+        oth, obox = oracle_tree_async(ops, w)
+    scene = svo.Octree(w["size"], w["brick_dim"])
+    scene.apply_ops(ops)
+    build_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream(dev)
+    s = stream.cuda_stream
+    scene.upload(s)
+    origins, dirs = make_rays(svo, w)
+    n = len(origins)
+    cols_host = [np.ascontiguousarray(origins[:, i]) for i in range(3)] + [np.ascontiguousarray(dirs[:, i])
+                                                                          for i in range(3)]
+    rays_dev = {k: torch.from_numpy(c).to(dev) for k, c in zip(RAY_KEYS, cols_host)}
+    outs = device_outputs(torch, svo, n, dev, OUT_FIELDS)
+    rp = {k: v.data_ptr() for k, v in rays_dev.items()}
+    hp = {k: v.data_ptr() for k, v in outs.items()}
+    checks = []  # (label, host results) compared with the oracle at the end
+
+    # camera rays in raster order: svo_cast_rows hands warps 8 x 4 blocks of neighbouring pixels
+    row = ray_rows(w)
+    clocks = ClockSampler(local_rank).start()  # samples from the warm-up on, so short timed regions get samples
+    for _ in range(args.warmup):
+        scene.cast(rp, hp, n, s, row_length=row)
+    torch.cuda.synchronize()
+
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        scene.cast(rp, hp, n, s, row_length=row)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if pg:
+        pg.barrier()
+    ms = max_over_ranks(ms, pg)
+    ms_step = ms / args.steps
+    value = n * world / (ms_step / 1e3) / 1e6
+    if want_check:
+        checks.append(("timed launch (%s)" % ("svo_cast_rows" if row else "svo_cast"), host_fields(svo, outs)))
+
+    # the instrumented cast: every field and the counters (algorithmic bytes of one launch)
+    full = device_outputs(torch, svo, n, dev, list(svo.HIT_FIELDS))
+    scene.cast(rp, {k: v.data_ptr() for k, v in full.items()}, n, s, row_length=row)
+    torch.cuda.synchronize()
+    visits, creads, vreads, runs = (int(full[k].to(torch.int64).sum()) for k in COUNTERS)
+    hits = int((full["status"] == 1).sum())
+    alg_bytes = alg_bytes_of(visits - runs, creads, vreads, hits)
+    if want_check:
+        checks.append(("instrumented launch, every field and counter", host_fields(svo, full)))
+    del full
+
+    # the same rays through plain svo_cast (warps take 32 consecutive rays of one row)
+    plain = None
+    if row:
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            scene.cast(rp, hp, n, s)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pms = max_over_ranks(e0.elapsed_time(e1), pg) / args.steps
+        plain = {"value": round(n * world / (pms / 1e3) / 1e6, 3), "ms_per_step": round(pms, 4)}
+        if want_check:
+            checks.append(("svo_cast, plain ray order", host_fields(svo, outs)))
+
+    variants = None
+    if not args.no_variants:
+        ws = svo.BatchWorkspace()
+        items = [(scene, rp, n, hp, row)]
+        sweep = sweep_batched(svo, torch, ws, items, stream, row)
+        (block, chunk, shape, sort), _ = min(sweep, key=lambda t: t[1])
+        cfg = svo.LaunchConfig(block, chunk, 0, shape, sort)
+        bms = interleaved_repeats({"b": lambda: ws.cast(items, cfg, s)}, args.steps, 1, stream, torch)["b"][0]
+        variants = {"persistent_autotuned": {"value": round(n / (bms / 1e3) / 1e6, 3), "unit": "Mrays/s",
+                                             "ms_per_step": round(bms, 4), "block": block, "rays_per_chunk": chunk,
+                                             "block_shape": shape, "sort_key": sort,
+                                             "launches_per_step": batched_launches(items, sort)},
+                    "sweep_ms": {"%dx%dx%dx%d" % k: round(v, 3) for k, v in sweep}}
+        if want_check:
+            checks.append(("persistent batched kernel, autotuned", host_fields(svo, outs)))
+    clk = clocks.stop()
+
+    # end to end through the host-buffer C-ABI call (pinned host memory)
+    pin_cols = [torch.from_numpy(c).pin_memory() for c in cols_host]
+    pin_out = {k: torch.empty(n, dtype=outs[k].dtype).pin_memory() for k in OUT_FIELDS}
+    cols_np = [c.numpy() for c in pin_cols]
+    out_np = {k: v.numpy().view(svo.HIT_FIELDS[k]) for k, v in pin_out.items()}
+    for _ in range(max(1, args.warmup)):
+        scene.cast_host_soa(cols_np, out_np, s, row_length=row)
+    if pg:
+        pg.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        scene.cast_host_soa(cols_np, out_np, s, row_length=row)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, pg)
+    e2e_value = n * world * args.steps / e2e_s / 1e6
+    if want_check:
+        checks.append(("host buffers (svo_cast_host%s)" % ("_rows" if row else ""), {k: v.copy() for k, v in out_np.items()}))
+    # the two ways svo_cast_host can move the data (svo_set_host_transfer), each timed the same way
+    e2e_paths = {}
+    for mode, name in ((1, "staged_copies"), (2, "direct_host_access")):
+        if svo.lib().svo_set_host_transfer(mode) != 0:
+            e2e_paths[name] = None
+            continue
+        scene.cast_host_soa(cols_np, out_np, s, row_length=row)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            scene.cast_host_soa(cols_np, out_np, s, row_length=row)
+        e2e_paths[name] = round(n * world * args.steps / max_over_ranks(time.perf_counter() - t0, pg) / 1e6, 3)
+        if want_check:
+            checks.append(("host buffers, %s" % name, {k: v.copy() for k, v in out_np.items()}))
+    svo.lib().svo_set_host_transfer(0)
+
+    # the oracle casts the whole batch once (all host threads): the CPU baseline and the parity reference
+    cpu, parity = None, None
+    if want_check:
+        oth.join()
+        tree = obox["tree"]
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        ref = tree.cast(origins, dirs, threads=threads)
+        cpu_s = time.perf_counter() - t0
+        cpu = {"value": round(n / cpu_s / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": "the whole %d-ray batch, once (%.1fs on %d threads)" % (n, cpu_s, threads)}
+        parity = merge_parity([compare_hits(got, ref, label) for label, got in checks])
+        del ref
+    checks.clear()
+
+    peak, peak_src = measured_peak()
+    achieved = alg_bytes / (ms_step / 1e3) / 1e9
+    prof = profile_traffic(workload)
+    traffic = prof.get("dram_bytes_per_launch")
+    l2 = None
+    if prof.get("l2_bytes_per_launch"):
+        l2 = {"bytes_per_launch": prof["l2_bytes_per_launch"],
+              "gbs": round(prof["l2_bytes_per_launch"] / (ms_step / 1e3) / 1e9, 1),
+              "hit_rate_pct": prof.get("l2_hit_rate_pct"), "l1_hit_rate_pct": prof.get("l1_hit_rate_pct"),
+              "frac_of_l2_peak": round(prof["l2_throughput_pct_of_peak"] / 100.0, 4),
+              "source": "ncu capture of one launch (profiles/); gbs with this run's kernel time"}
+    io_bytes = n * 24 + n * sum(OUT_BYTES.values())
+    st = scene.stats()
+    rec = {
+        "metric": "Mrays/s", "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload, "octree": "%d^3" % w["size"], "brick_dim": w["brick_dim"],
+                   "rays_per_step": n, "hit_rate": round(hits / n, 4), "nodes": st["nodes"],
+                   "per_ray": {"node_visits": round(visits / n, 2), "child_reads": round(creads / n, 2),
+                               "voxel_reads": round(vreads / n, 2), "restart_run_visits": round(runs / n, 2)},
+                   "parted_bricks": st["parted_bricks"], "voxels_inserted": int(len(ops)),
+                   "l2": "inputs larger than L2 (rays %.0f MB + hits %.0f MB per step); the %.0f MB scene image "
+                         "stays resident" % (n * 24 / 1e6, n * sum(OUT_BYTES.values()) / 1e6, st["device_bytes"] / 1e6),
+                   "build_s": round(build_s, 1), "parallelism": "replicas" if world > 1 else "single",
+                   "ray_order": ("rows of %d rays (svo_cast_rows: 8 x 4 ray blocks per warp)" % row) if row
+                   else "as generated (svo_cast)",
+                   "svo_cast_plain_order": plain},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_src,
+                     "alg_bytes_per_launch": alg_bytes, "alg_bytes_per_ray": round(alg_bytes / n, 2),
+                     "io_bytes_per_launch": io_bytes,
+                     "io_note": "rays in (24 B) and hit fields out (34 B) per ray: DRAM traffic that the "
+                                "algorithmic bytes (scene reads) do not count", "l2": l2},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": n * 24,
+                "d2h_bytes_per_step": n * sum(OUT_BYTES.values()), "paths": e2e_paths},
+        "gpu_launches": args.steps,
+        "clocks": clk,
+        "variants": variants,
+        "parity": parity,
+    }
+    del outs, rays_dev
+    torch.cuda.empty_cache()
+    return rec, pg
 
 
+# ---- north star (a): incoherent rays, plain cast vs batched forms ---------------------------------
+def north_star_incoherent(args):
+    """incoherent1024: plain svo_cast against the autotuned persistent batched cast in index order and
+    with the ray sort, timed over interleaved repeats, every variant's hits checked against the oracle."""
+    import torch
+    import shocovox_gb300 as svo
+    w = WORKLOADS["incoherent1024"]
+    dev = torch.device("cuda", 0)
+    t0 = time.perf_counter()
+    ops = scene_ops(svo, w)
+    oth, obox = oracle_tree_async(ops, w)
+    scene = svo.Octree(w["size"], w["brick_dim"])
+    scene.apply_ops(ops)
+    build_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream(dev)
+    s = stream.cuda_stream
+    scene.upload(s)
+    origins, dirs = make_rays(svo, w)
+    n = len(origins)
+    rays = {k: torch.from_numpy(np.ascontiguousarray(a[:, i])).to(dev)
+            for a, names in ((origins, RAY_KEYS[:3]), (dirs, RAY_KEYS[3:])) for i, k in enumerate(names)}
+    rp = {k: v.data_ptr() for k, v in rays.items()}
+    outs = {v: device_outputs(torch, svo, n, dev, OUT_FIELDS) for v in ("plain", "index_order", "sorted")}
+    hp = {v: {k: t.data_ptr() for k, t in o.items()} for v, o in outs.items()}
+    ws = svo.BatchWorkspace()
+    items = {v: [(scene, rp, n, hp[v], 0)] for v in ("index_order", "sorted")}
+    sweep = sweep_batched(svo, torch, ws, items["index_order"], stream, 0)
+    best = {}
+    for v, key in (("index_order", 0), ("sorted", 1)):
+        (b, c, sh, so), _ = min((t for t in sweep if t[0][3] == key), key=lambda t: t[1])
+        best[v] = svo.LaunchConfig(b, c, 0, sh, so)
+    clocks = ClockSampler(0).start()
+    for _ in range(args.warmup):
+        scene.cast(rp, hp["plain"], n, s)
+    reps = interleaved_repeats({"plain": lambda: scene.cast(rp, hp["plain"], n, s),
+                                "index_order": lambda: ws.cast(items["index_order"], best["index_order"], s),
+                                "sorted": lambda: ws.cast(items["sorted"], best["sorted"], s)},
+                               args.steps, REPEATS, stream, torch)
+    clk = clocks.stop()
+    got = {v: host_fields(svo, o) for v, o in outs.items()}
+    oth.join()
+    t0 = time.perf_counter()
+    ref = obox["tree"].cast(origins, dirs, threads=os.cpu_count() or 1)
+    cpu_s = time.perf_counter() - t0
+    parity = merge_parity([compare_hits(got[v], ref, v) for v in got])
+    plain = spread(n, reps["plain"])
+    res = {"svo_cast": plain}
+    for v in ("index_order", "sorted"):
+        c = best[v]
+        res["batched_" + v] = dict(spread(n, reps[v]), block=c.block, rays_per_chunk=c.rays_per_chunk,
+                                   sort_key=c.sort_key, launches_per_step=batched_launches(items[v], c.sort_key),
+                                   vs_plain=versus(spread(n, reps[v]), plain))
+    del outs, rays
+    torch.cuda.empty_cache()
+    return {"workload": "incoherent1024 (1024^3, brick 8, ~5% occupancy, 2^22 rays from the bounding sphere in "
+                        "uniform directions)", "rays_per_step": n, "unit": "Mrays/s", "build_s": round(build_s, 1),
+            "steps_per_repeat": args.steps, "variants": res,
+            "l2": "rays 100 MB + hit fields 143 MB per step (larger than L2)",
+            "cpu_oracle": {"value": round(n / cpu_s / 1e6, 3), "unit": "Mrays/s", "cores": os.cpu_count() or 1},
+            "parity": parity, "clocks": clk}
+
+
+# ---- north star (b): many scenes in one persistent launch ------------------------------------------
 def multiscene_specs(w):
     """64 scenes: size from {64..512}^3, brick dim from {2,4,8}, occupancy 2-20%, noise + spheres,
     a log-uniform 1K-1M ray batch each (half camera rays, half random directions)."""
@@ -302,31 +659,50 @@ def multiscene_rays(svo, sp):
 
 
 def run_multiscene(args, w):
-    """Batched multi-scene cast: serial plain dispatch vs one persistent launch vs that launch in a CUDA graph."""
+    """Batched multi-scene cast: serial plain dispatch vs one persistent launch vs that launch in a CUDA
+    graph, repeated; every item's hits checked against the oracle's cast of the same rays."""
     import concurrent.futures as cf
     import torch
     import shocovox_gb300 as svo
+    from oracle import oracle
     from shocovox_gb300 import autotune
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(0)
     specs = multiscene_specs(w)
+    workers = min(16, os.cpu_count() or 4)
     t0 = time.perf_counter()
 
-    def build(sp):
-        ops = svo.gen_scene(sp["kind"], sp["size"], sp["brick_dim"], sp["seed"], occupancy=sp["occupancy"],
-                            spheres=sp["spheres"], octaves=sp["octaves"], base_freq=sp["base_freq"])
-        t = svo.Octree(sp["size"], sp["brick_dim"])
-        t.apply_ops(ops)
-        return t, len(ops)
+    def ops_of(sp):
+        return svo.gen_scene(sp["kind"], sp["size"], sp["brick_dim"], sp["seed"], occupancy=sp["occupancy"],
+                             spheres=sp["spheres"], octaves=sp["octaves"], base_freq=sp["base_freq"])
 
-    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
-        built = list(ex.map(build, specs))
+    all_ops = [ops_of(sp) for sp in specs]
+    gen_s = time.perf_counter() - t0
+
+    def build(i):
+        t = svo.Octree(specs[i]["size"], specs[i]["brick_dim"])
+        t.apply_ops(all_ops[i])
+        return t
+
+    def build_oracle(i):
+        t = oracle.Tree(specs[i]["size"], specs[i]["brick_dim"])
+        t.apply_ops(all_ops[i])
+        return t
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=workers) as ex:
+        built = list(ex.map(build, range(len(specs))))
     build_s = time.perf_counter() - t0
+    n_voxels = int(sum(len(o) for o in all_ops))
+    # the oracle trees build on the host threads while the GPU runs
+    opool = None
+    ofut = None
+    if not args.no_parity:
+        opool = cf.ThreadPoolExecutor(max_workers=workers)
+        ofut = [opool.submit(build_oracle, i) for i in range(len(specs))]
     stream = torch.cuda.current_stream(dev)
     s = stream.cuda_stream
-    tmap = {np.uint8: torch.uint8, np.uint32: torch.int32, np.float32: torch.float32}
     # one batch: every ray column and hit field is one buffer over all scenes, each scene a slice
-    ray_keys = ("ox", "oy", "oz", "dx", "dy", "dz")
     host_rays = [multiscene_rays(svo, sp) for sp in specs]
     counts = [len(r[0]) for r in host_rays]
     begins = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
@@ -334,72 +710,78 @@ def run_multiscene(args, w):
     all_o = np.concatenate([r[0] for r in host_rays])
     all_d = np.concatenate([r[1] for r in host_rays])
     host_cols = [np.ascontiguousarray(all_o[:, i]) for i in range(3)] + [np.ascontiguousarray(all_d[:, i]) for i in range(3)]
-    dev_cols = {k: torch.from_numpy(c).to(dev) for k, c in zip(ray_keys, host_cols)}
-    dev_out = {k: torch.empty(total, dtype=tmap[svo.HIT_FIELDS[k]], device=dev) for k in OUT_FIELDS}
+    dev_cols = {k: torch.from_numpy(c).to(dev) for k, c in zip(RAY_KEYS, host_cols)}
+    dev_out = device_outputs(torch, svo, total, dev, OUT_FIELDS)
     # per scene two items: its camera rays (rows of the image: cast in 8 x 4 ray blocks) and its
     # random rays
-    scenes, items, outs = [], [], []
-    for i, (t, _) in enumerate(built):
+    items = []
+    for i, t in enumerate(built):
         t.upload(s)
         a, b = int(begins[i]), int(begins[i + 1])
-        scenes.append(t)
-        outs.append({k: v[a:b] for k, v in dev_out.items()})
         ncam, row = host_rays[i][2], host_rays[i][3]
         for lo, hi, r in ((a, a + ncam, row), (a + ncam, b, 0)):
             if hi > lo:
-                rays = {k: v[lo:hi] for k, v in dev_cols.items()}
-                out = {k: v[lo:hi] for k, v in dev_out.items()}
-                items.append((t, {k: v.data_ptr() for k, v in rays.items()}, hi - lo,
-                              {k: v.data_ptr() for k, v in out.items()}, r))
+                items.append((t, {k: v[lo:hi].data_ptr() for k, v in dev_cols.items()}, hi - lo,
+                              {k: v[lo:hi].data_ptr() for k, v in dev_out.items()}, r))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-
-    def timed(fn, reps):
-        fn()
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(reps):
-            fn()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / reps
 
     def serial():
         for (t, rp, n, hp, row) in items:
             t.cast(rp, hp, n, s, row_length=row)
 
     ws = svo.BatchWorkspace()
-    bitems = items
-    cfg, tune_info = autotune.tune(ws, bitems, torch.cuda.get_device_name(0),
-                                   lambda c: timed(lambda: ws.cast(bitems, c, s), 2))
+
+    def time_cfg(c):
+        ws.cast(items, c, s)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(2):
+            ws.cast(items, c, s)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 2
+
+    cfg, tune_info = autotune.tune(ws, items, torch.cuda.get_device_name(0), time_cfg)
 
     def batched():
-        ws.cast(bitems, cfg, s)
+        ws.cast(items, cfg, s)
 
-    clocks = ClockSampler(0)
-    clocks.start()
-    for _ in range(args.warmup):
-        serial()
-        batched()
+    checks = []
+    serial()
     torch.cuda.synchronize()
-    serial_ms = timed(serial, args.steps)
-    ref_out = [{k: v.clone() for k, v in out.items()} for out in outs]
-    batched_ms = timed(batched, args.steps)
-    same = all(torch.equal(a[k], b[k]) for a, b in zip(ref_out, outs) for k in OUT_FIELDS)
+    checks.append(("serial plain launches", host_fields(svo, dev_out)))
+    dev_out_clear(dev_out)
+    batched()
+    torch.cuda.synchronize()
+    checks.append(("one batched launch", host_fields(svo, dev_out)))
     # one persistent launch captured in a CUDA graph (workspace already sized, blocks per SM fixed)
     if cfg.blocks_per_sm == 0:
         per_sm = {64: 14, 96: 9, 128: 7}.get(cfg.block, 2)  # resident blocks at 72 registers per thread
         gcfg = svo.LaunchConfig(cfg.block, cfg.rays_per_chunk, per_sm, cfg.block_shape, cfg.sort_key)
     else:
         gcfg = cfg
+    gws = svo.BatchWorkspace()  # the graph keeps its own workspace: later casts on `ws` leave it alone
     gstream = torch.cuda.Stream(dev)
     graph = torch.cuda.CUDAGraph()
     with torch.cuda.stream(gstream):
-        ws.cast(bitems, gcfg, gstream.cuda_stream)
+        gws.cast(items, gcfg, gstream.cuda_stream)
         torch.cuda.synchronize()
         with torch.cuda.graph(graph, stream=gstream):
-            ws.cast(bitems, gcfg, gstream.cuda_stream)
+            gws.cast(items, gcfg, gstream.cuda_stream)
     torch.cuda.synchronize()
-    graph_ms = timed(graph.replay, args.steps)
+    dev_out_clear(dev_out)
+    graph.replay()
+    torch.cuda.synchronize()
+    checks.append(("batched launch replayed from a CUDA graph", host_fields(svo, dev_out)))
+
+    clocks = ClockSampler(0).start()
+    for _ in range(args.warmup):
+        serial()
+        batched()
+        graph.replay()
+    torch.cuda.synchronize()
+    reps = interleaved_repeats({"serial": serial, "batched": batched, "graph": graph.replay}, args.steps,
+                               REPEATS, stream, torch)
     clk = clocks.stop()
 
     # algorithmic bytes of the batch, from the instrumented batched cast
@@ -412,34 +794,17 @@ def run_multiscene(args, w):
     sums = {k: sum(int(c[k].to(torch.int64).sum()) for c in cnt) for k in COUNTERS}
     hits = sum(int((c["status"] == 1).sum()) for c in cnt)
     alg = alg_bytes_of(sums["node_visits"] - sums["run_visits"], sums["child_reads"], sums["voxel_reads"], hits)
+    del cnt
 
-    # end to end: host rays in, one batched launch, host hits out (pinned buffers, copies in the timed region;
-    # one copy per ray column and per hit field of the whole batch)
-    pin_in = {k: torch.from_numpy(c).pin_memory() for k, c in zip(ray_keys, host_cols)}
-    pin_out = {k: torch.empty(total, dtype=tmap[svo.HIT_FIELDS[k]]).pin_memory() for k in OUT_FIELDS}
-
-    def e2e():
-        for k in ray_keys:
-            dev_cols[k].copy_(pin_in[k], non_blocking=True)
-        ws.cast(bitems, cfg, s)
-        for k in OUT_FIELDS:
-            pin_out[k].copy_(dev_out[k], non_blocking=True)
-
-    e2e()
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e()
-    torch.cuda.synchronize()
-    e2e_serial_s = (time.perf_counter() - t1) / args.steps
-    serial_hits = {k: v.clone() for k, v in pin_out.items()}
-
-    # the same with the batch cut into 4 groups of consecutive items, each on its own stream with its
-    # own workspace: one group's copies overlap another group's launch
+    # end to end: host rays in, batched launches, host hits out (pinned buffers, copies in the timed region):
+    # the batch cut into 4 groups of consecutive items, each copy-in, launch and copy-out on its own stream
+    # with its own workspace, so one group's copies overlap another group's launch
+    pin_in = {k: torch.from_numpy(c).pin_memory() for k, c in zip(RAY_KEYS, host_cols)}
+    pin_out = {k: torch.empty(total, dtype=v.dtype).pin_memory() for k, v in dev_out.items()}
     base = dev_cols["ox"].data_ptr()
-    offs = [(it[1]["ox"] - base) // 4 for it in bitems]
+    offs = [(it[1]["ox"] - base) // 4 for it in items]
     n_groups, groups, cur_g, acc = 4, [], [], 0
-    for it, off in zip(bitems, offs):
+    for it, off in zip(items, offs):
         cur_g.append((it, off))
         acc += it[2]
         if len(groups) < n_groups - 1 and acc >= total * (len(groups) + 1) / n_groups:
@@ -457,7 +822,7 @@ def run_multiscene(args, w):
         for g, (lo, hi), st, wsg in zip(groups, g_ranges, g_streams, g_ws):
             st.wait_event(g_start)
             with torch.cuda.stream(st):
-                for k in ray_keys:
+                for k in RAY_KEYS:
                     dev_cols[k][lo:hi].copy_(pin_in[k][lo:hi], non_blocking=True)
                 wsg.cast([it for it, _ in g], cfg, st.cuda_stream)
                 for k in OUT_FIELDS:
@@ -472,46 +837,50 @@ def run_multiscene(args, w):
         e2e_groups()
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t1) / args.steps
-    groups_same = all(torch.equal(serial_hits[k], pin_out[k]) for k in OUT_FIELDS)
+    checks.append(("host buffers, 4 pipelined groups", {k: v.numpy().view(svo.HIT_FIELDS[k]).copy()
+                                                        for k, v in pin_out.items()}))
 
-    cpu = None
-    if not args.no_cpu_baseline:
-        from oracle import oracle
-        # a bounded sample: the 8 cheapest scenes to rebuild on the CPU, 20k rays each at most
-        order = sorted(range(len(specs)), key=lambda i: built[i][1])[:8]
-        rays_done, secs = 0, 0.0
+    # every item against the oracle's cast of its rays
+    parity, cpu = None, None
+    if ofut is not None:
+        trees = [f.result() for f in ofut]
+        opool.shutdown()
         threads = os.cpu_count() or 1
-        for i in order:
-            sp = specs[i]
-            ops = svo.gen_scene(sp["kind"], sp["size"], sp["brick_dim"], sp["seed"], occupancy=sp["occupancy"],
-                                spheres=sp["spheres"], octaves=sp["octaves"], base_freq=sp["base_freq"])
-            ot = oracle.Tree(sp["size"], sp["brick_dim"])
-            ot.apply_ops(ops)
-            o, d = host_rays[i][:2]
-            step = max(1, len(o) // 20000)
-            tt = time.perf_counter()
-            ot.cast(o[::step], d[::step], threads=threads)
-            secs += time.perf_counter() - tt
-            rays_done += len(o[::step])
-        cpu = {"value": round(rays_done / secs / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
-               "sample": "%d rays over the 8 smallest of the 64 scenes" % rays_done}
+        ref = {k: np.zeros(total, dtype=t) for k, t in oracle.HIT_FIELDS.items()}
+        cpu_s = 0.0
+        for i, tr in enumerate(trees):
+            a, b = int(begins[i]), int(begins[i + 1])
+            t0 = time.perf_counter()
+            r = tr.cast(all_o[a:b], all_d[a:b], threads=threads)
+            cpu_s += time.perf_counter() - t0
+            for k in ref:
+                ref[k][a:b] = r[k]
+        del trees
+        parity = merge_parity([compare_hits(got, ref, label) for label, got in checks])
+        parity["items_checked"] = len(items)
+        cpu = {"value": round(total / cpu_s / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": "every ray of the 64 scenes, once (%.1fs on %d threads)" % (cpu_s, threads)}
+    checks.clear()
 
     peak, peak_src = measured_peak()
-    print(json.dumps({
-        "metric": "Mrays/s", "value": round(total / (graph_ms / 1e3) / 1e6, 3), "unit": "Mrays/s", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(graph_ms, 4), "higher_is_better": True,
+    graph_sp, serial_sp, batched_sp = spread(total, reps["graph"]), spread(total, reps["serial"]), spread(total, reps["batched"])
+    graph_ms = graph_sp["ms_per_step"]
+    rec = {
+        "metric": "Mrays/s", "value": graph_sp["value"], "unit": "Mrays/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": graph_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "multiscene64", "scenes": len(specs), "rays_per_step": total,
+        "config": {"workload": "multiscene64", "scenes": len(specs), "items": len(items), "rays_per_step": total,
                    "sizes": sorted({sp["size"] for sp in specs}), "brick_dims": sorted({sp["brick_dim"] for sp in specs}),
-                   "voxels_inserted": int(sum(b[1] for b in built)), "build_s": round(build_s, 1),
+                   "voxels_inserted": n_voxels, "gen_s": round(gen_s, 1), "build_s": round(build_s, 1),
                    "l2": "rays %.0f MB + hits %.0f MB per step (larger than L2)" % (total * 24 / 1e6, total * 34 / 1e6),
-                   "timed": "the batched cast replayed from a CUDA graph (one persistent launch; with sort_key 1 the ray sort's six launches too)",
+                   "timed": "the batched cast replayed from a CUDA graph (one persistent launch; with sort_key 1 the "
+                            "ray sort's six launches too), median of %d repeats of %d steps" % (REPEATS, args.steps),
                    "ray_order": "per scene: camera rays as rows of the image (8 x 4 ray blocks per warp), "
                                 "random rays in order or sorted by direction octant and entry point (autotune.sort_key)",
-                   "serial_plain": {"value": round(total / (serial_ms / 1e3) / 1e6, 3), "ms_per_step": round(serial_ms, 4),
-                                    "launches_per_step": len(items)},
-                   "batched": {"value": round(total / (batched_ms / 1e3) / 1e6, 3), "ms_per_step": round(batched_ms, 4)},
-                   "batched_equals_serial": bool(same),
+                   "graph": graph_sp,
+                   "serial_plain": dict(serial_sp, launches_per_step=len(items)),
+                   "batched": batched_sp,
+                   "graph_vs_serial": versus(graph_sp, serial_sp),
                    "autotune": {"block": cfg.block, "rays_per_chunk": cfg.rays_per_chunk, "block_shape": cfg.block_shape,
                                 "sort_key": cfg.sort_key, "cached": tune_info["cached"],
                                 "sweep_ms": tune_info.get("sweep_ms")}},
@@ -521,109 +890,231 @@ def run_multiscene(args, w):
         "cpu_baseline": cpu,
         "e2e": {"value": round(total / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": total * 24,
                 "d2h_bytes_per_step": total * sum(OUT_BYTES.values()),
-                "how": "4 groups of items, each copy-in, batched launch, copy-out on its own stream",
-                "one_stream": round(total / e2e_serial_s / 1e6, 3), "same_hits_as_one_stream": bool(groups_same)},
-        "gpu_launches": args.steps * batched_launches(bitems, gcfg.sort_key),
+                "how": "4 groups of items, each copy-in, batched launch, copy-out on its own stream"},
+        "gpu_launches": args.steps * batched_launches(items, gcfg.sort_key),
         "clocks": clk,
-    }))
+        "parity": parity,
+    }
+    del dev_cols, dev_out, graph
+    torch.cuda.empty_cache()
+    return rec
 
 
-def run_served(args, w):
-    """Served load: Poisson camera requests over 16 resident scenes, continuous batching vs serial dispatch."""
-    import torch
-    import shocovox_gb300 as svo
-    torch.cuda.set_device(0)
+def dev_out_clear(d):
+    for v in d.values():
+        v.zero_()
+
+
+# ---- north star (c): served requests --------------------------------------------------------------
+SERVE_STRIDE = 1024  # every request: its pixels first, first + 1024, ... are checked against the oracle
+SERVE_FULL_EVERY = 500  # every 500th request also returns every hit field and is checked in full
+SERVE_FIELDS = ("status", "albedo")  # what every request returns to host memory
+
+
+def served_scenes(svo, w):
     rng = np.random.default_rng(w["seed"])
     sizes = [int(v) for v in rng.permutation(np.repeat([256, 512, 1024, 2048], w["served"] // 4))]
-    t0 = time.perf_counter()
-    scenes = []
-    for i, S in enumerate(sizes):
-        ops = svo.gen_scene(4, S, 8, w["seed"] + 31 * i, occupancy=float(rng.uniform(0.01, 0.05)))
-        t = svo.Octree(S, 8)
-        t.apply_ops(ops)
-        scenes.append(t)
-    build_s = time.perf_counter() - t0
+    recipes = [(S, w["seed"] + 31 * i, float(rng.uniform(0.01, 0.05))) for i, S in enumerate(sizes)]
+    return rng, sizes, recipes
+
+
+def served_requests(rng, sizes, w):
     n_req = w["requests"]
     arrivals = np.cumsum(rng.exponential(1.0 / w["rate"], n_req))
     reqs = []
-    for k in range(n_req):
-        j = int(rng.integers(0, len(scenes)))
+    for _ in range(n_req):
+        j = int(rng.integers(0, len(sizes)))
         S = float(sizes[j])
         a, el = rng.uniform(0, 2 * np.pi), rng.uniform(0.35, 0.7)
         eye = [S / 2 + 1.4 * S * np.cos(el) * np.cos(a), S / 2 + 1.4 * S * np.sin(el), S / 2 + 1.4 * S * np.cos(el) * np.sin(a)]
         target = [S / 2 + rng.uniform(-0.1, 0.1) * S, S / 2, S / 2 + rng.uniform(-0.1, 0.1) * S]
         wd, ht = RESOLUTIONS[int(rng.integers(0, len(RESOLUTIONS)))]
         reqs.append((j, eye, target, 60.0, wd, ht))
+    return arrivals, reqs
+
+
+def run_served(args, w):
+    """Served load: Poisson camera requests over 16 scenes under a device budget that forces evictions,
+    continuous batching vs serial dispatch, paced and at capacity, repeated; every request checked against
+    the oracle on a strided sample of its pixels, every 500th request on all of its pixels and fields."""
+    import concurrent.futures as cf
+    import torch
+    import shocovox_gb300 as svo
+    from oracle import oracle
+    torch.cuda.set_device(0)
+    rng, sizes, recipes = served_scenes(svo, w)
+    t0 = time.perf_counter()
+    all_ops = [svo.gen_scene(4, S, 8, seed, occupancy=occ) for S, seed, occ in recipes]
+    scenes = []
+    for (S, _, _), ops in zip(recipes, all_ops):
+        t = svo.Octree(S, 8)
+        t.apply_ops(ops)
+        scenes.append(t)
+    build_s = time.perf_counter() - t0
+    # device image of every scene, measured by one upload
+    image = []
+    for t in scenes:
+        t.upload()
+        image.append(int(t.stats()["device_bytes"]))
+        t.release_device()
+    budget = int(w["budget_frac"] * sum(image))
+    arrivals, reqs = served_requests(rng, sizes, w)
+    n_req = len(reqs)
     total_rays = sum(r[4] * r[5] for r in reqs)
-    # pinned result buffers (status + albedo per ray), reused round-robin by later requests
+    firsts = [(k * 7919) % SERVE_STRIDE for k in range(n_req)]
+    full_ids = list(range(0, n_req, SERVE_FULL_EVERY))
+
+    # oracle references (built and cast on host threads while nothing runs on the GPU)
+    oref_sample, oref_full = None, None
+    if not args.no_parity:
+        def build_oracle(i):
+            t = oracle.Tree(recipes[i][0], 8)
+            t.apply_ops(all_ops[i])
+            return t
+        with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+            otrees = list(ex.map(build_oracle, range(len(scenes))))
+        threads = os.cpu_count() or 1
+        oref_sample = [None] * n_req
+        for j, tr in enumerate(otrees):
+            ks = [k for k, r in enumerate(reqs) if r[0] == j]
+            if not ks:
+                continue
+            o_d = [oracle.gen_camera_rays_strided(reqs[k][1], reqs[k][2], reqs[k][3], reqs[k][4], reqs[k][5], firsts[k],
+                                                  SERVE_STRIDE) for k in ks]
+            r = tr.cast(np.concatenate([x[0] for x in o_d]), np.concatenate([x[1] for x in o_d]), threads=threads)
+            at = 0
+            for k, x in zip(ks, o_d):
+                m = len(x[0])
+                oref_sample[k] = {f: r[f][at:at + m] for f in SERVE_FIELDS}
+                at += m
+        oref_full = {}
+        for k in full_ids:
+            j, eye, target, fov, wd, ht = reqs[k]
+            o, d = oracle.gen_camera_rays(eye, target, fov, wd, ht)
+            oref_full[k] = otrees[j].cast(o, d, threads=threads)
+        del otrees
+
+    # pinned result buffers (SERVE_FIELDS per ray), reused round-robin by later requests; the full-record
+    # requests get buffers of their own with every field
     ring = 48
     maxn = max(r[4] * r[5] for r in reqs)
     bufs = [{"status": torch.empty(maxn, dtype=torch.uint8).pin_memory().numpy(),
-             "albedo": torch.empty(maxn, dtype=torch.int32).pin_memory().numpy()} for _ in range(ring)]
+             "albedo": torch.empty(maxn, dtype=torch.int32).pin_memory().numpy().view(np.uint32)} for _ in range(ring)]
+    full_fields = ID_FIELDS + FLOAT_FIELDS
+    tnp = {np.uint8: torch.uint8, np.uint32: torch.int32, np.float32: torch.float32}
+    full_bufs = {k: {f: torch.empty(reqs[k][4] * reqs[k][5], dtype=tnp[svo.HIT_FIELDS[f]]).pin_memory().numpy().view(
+        svo.HIT_FIELDS[f]) for f in full_fields} for k in full_ids}
 
     def serve(srv, paced):
         ids = [srv.add_scene(t) for t in scenes]
         assert ids == list(range(len(scenes)))
-        # warm-up: every scene resident and the launch path exercised once
+        # warm-up: the launch path exercised once per scene (scenes past the budget are evicted again)
         for j in range(len(scenes)):
             srv.wait(srv.submit(j, [0.0, float(sizes[j]), 0.0], [sizes[j] / 2] * 3, 60.0, 64, 64,
                                 out={k: v[:4096] for k, v in bufs[0].items()}))
+        st0 = srv.stats()
+        sample = [None] * n_req
         start = srv.now()
-        rids, res = [], [None] * len(reqs)
+        rids, res = [], [None] * n_req
+
+        def out_of(k):  # the host arrays request k writes
+            if k in full_bufs:
+                return full_bufs[k]
+            return {f: v[:reqs[k][4] * reqs[k][5]] for f, v in bufs[k % ring].items()}
+
+        def finish(k):
+            res[k] = srv.wait(rids[k], 600.0)
+            b = out_of(k)
+            sample[k] = {f: b[f][firsts[k]::SERVE_STRIDE].copy() for f in SERVE_FIELDS}
+
         for k, r in enumerate(reqs):
             if k >= ring:  # the result buffers of request k - ring are reused: it must be done
-                res[k - ring] = srv.wait(rids[k - ring], 600.0)
+                finish(k - ring)
             if paced:
                 delay = start + arrivals[k] - srv.now()
                 if delay > 0:
                     time.sleep(delay)
-            out = {kk: v[:r[4] * r[5]] for kk, v in bufs[k % ring].items()}
-            rids.append(srv.submit(*r, out=out))
-        for k in range(max(0, len(reqs) - ring), len(reqs)):
-            res[k] = srv.wait(rids[k], 600.0)
-        lat = np.array([x["done_s"] - x["submit_s"] for x in res])
-        span = max(x["done_s"] for x in res) - min(x["submit_s"] for x in res)
+            rids.append(srv.submit(*r, out=out_of(k)))
+        for k in range(max(0, n_req - ring), n_req):
+            finish(k)
+        if paced:  # from the scheduled arrival: a submission the loop made late still counts its wait
+            lat = np.array([x["done_s"] - (start + arrivals[k]) for k, x in enumerate(res)])
+        else:
+            lat = np.array([x["done_s"] - x["submit_s"] for x in res])
+        span = max(x["done_s"] for x in res) - (start if paced else min(x["submit_s"] for x in res))
         st = srv.stats()
         srv.close()
-        return {"value": round(total_rays / span / 1e6, 3), "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 2),
-                "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 2), "span_s": round(span, 3),
-                "launches": st["launches"], "uploads": st["uploads"], "evictions": st["evictions"],
-                "mean_batch": round(float(np.mean([x["batch_requests"] for x in res])), 2)}
+        checks = []
+        if oref_sample is not None:
+            got = {f: np.concatenate([sample[k][f] for k in range(n_req)]) for f in SERVE_FIELDS}
+            ref = {f: np.concatenate([oref_sample[k][f] for k in range(n_req)]) for f in SERVE_FIELDS}
+            checks.append(compare_hits(got, ref, "every request, pixels first + 1024 i (status, albedo)"))
+            for k in full_ids:
+                checks.append(compare_hits(full_bufs[k], oref_full[k], "request %d, every pixel and field" % k))
+        return {"value": round(total_rays / span / 1e6, 3), "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
+                "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3), "span_s": round(span, 3),
+                "launches": st["launches"] - st0["launches"], "uploads": st["uploads"] - st0["uploads"],
+                "evictions": st["evictions"] - st0["evictions"],
+                "mean_batch": round(float(np.mean([x["batch_requests"] for x in res])), 2),
+                "parity": merge_parity(checks)}
 
-    # latency-bound: clock samples once a second (each nvidia-smi query is a driver call on the host)
-    clocks = ClockSampler(0, interval_ms=1000)
-    clocks.start()
-    budget = int(w["budget_gb"] * (1 << 30))
-    # paced load: launches of at most 4 M rays keep a large request from delaying the next ones
-    batched = serve(svo.Server(budget_bytes=budget, max_batch_requests=64, max_batch_rays=1 << 22, max_inflight=3),
-                    paced=True)
-    serial = serve(svo.Server(budget_bytes=budget, max_batch_requests=1, max_inflight=1), paced=True)
-    # capacity: the same requests submitted as fast as result buffers free up (48 in flight)
-    batched_cap = serve(svo.Server(budget_bytes=budget, max_batch_requests=64, max_batch_rays=1 << 25,
-                                   max_inflight=3), paced=False)
-    serial_cap = serve(svo.Server(budget_bytes=budget, max_batch_requests=1, max_inflight=1), paced=False)
+    clocks = ClockSampler(0, interval_ms=500).start()
+    runs = {"served": [], "serial_dispatch": [], "capacity_served": [], "capacity_serial_dispatch": []}
+    for _ in range(w["repeats"]):
+        # paced: launches of at most 4 M rays keep a large request from delaying the next ones
+        runs["served"].append(serve(svo.Server(budget_bytes=budget, max_batch_requests=64, max_batch_rays=1 << 22,
+                                               max_inflight=3), paced=True))
+        runs["serial_dispatch"].append(serve(svo.Server(budget_bytes=budget, max_batch_requests=1, max_inflight=1),
+                                             paced=True))
+        # capacity: the same requests submitted as fast as result buffers free up (48 outstanding)
+        runs["capacity_served"].append(serve(svo.Server(budget_bytes=budget, max_batch_requests=64,
+                                                        max_batch_rays=1 << 25, max_inflight=3), paced=False))
+        runs["capacity_serial_dispatch"].append(serve(svo.Server(budget_bytes=budget, max_batch_requests=1,
+                                                                 max_inflight=1), paced=False))
     clk = clocks.stop()
-    print(json.dumps({
-        "metric": "Mrays/s", "value": batched["value"], "unit": "Mrays/s", "n_gpus": 1, "steps": n_req, "warmup": len(scenes),
-        "ms_per_step": round(batched["span_s"] / n_req * 1e3, 4), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+
+    def summary(rs):
+        v = np.array([r["value"] for r in rs])
+        return {"value": round(float(np.median(v)), 3), "min": round(float(v.min()), 3), "max": round(float(v.max()), 3),
+                "p50_ms": round(float(np.median([r["p50_ms"] for r in rs])), 3),
+                "p99_ms": round(float(np.median([r["p99_ms"] for r in rs])), 3),
+                "p99_ms_per_repeat": [r["p99_ms"] for r in rs], "repeats": len(rs),
+                "uploads": [r["uploads"] for r in rs], "evictions": [r["evictions"] for r in rs],
+                "launches": [r["launches"] for r in rs], "span_s": [r["span_s"] for r in rs],
+                "mean_batch": [r["mean_batch"] for r in rs]}
+
+    sm = {k: summary(v) for k, v in runs.items()}
+    parity = merge_parity([r["parity"] for v in runs.values() for r in v])
+    srv_ = sm["served"]
+    return {
+        "metric": "Mrays/s", "value": srv_["value"], "unit": "Mrays/s", "n_gpus": 1, "steps": n_req,
+        "warmup": len(scenes), "ms_per_step": round(float(np.median([r["span_s"] for r in runs["served"]])) / n_req * 1e3, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "served16", "scenes": len(scenes), "sizes": sizes, "requests": n_req,
-                   "arrival_rate_per_s": w["rate"], "rays": total_rays, "budget_gb": w["budget_gb"],
-                   "build_s": round(build_s, 1), "outputs": "status + albedo per ray, to pinned host memory",
-                   "server_config": {"paced": "max_batch_requests 64, max_batch_rays 2^22, max_inflight 3",
-                                     "capacity": "max_batch_requests 64, max_batch_rays 2^25, max_inflight 3",
-                                     "serial_dispatch": "max_batch_requests 1, max_inflight 1"},
-                   "served": batched, "serial_dispatch": serial,
-                   "capacity": {"note": "all requests queued, 48 outstanding", "served": batched_cap,
-                                "serial_dispatch": serial_cap},
-                   "p50_ms": batched["p50_ms"], "p99_ms": batched["p99_ms"]},
+                   "arrival_rate_per_s": w["rate"], "rays": total_rays, "build_s": round(build_s, 1),
+                   "scene_image_bytes": image, "budget_bytes": budget,
+                   "budget": "half the sum of the 16 scene images, so scenes are evicted and uploaded again while "
+                             "requests run (the box-recipe scenes total %.1f MB)" % (sum(image) / 1e6),
+                   "outputs": "status + albedo of every pixel to pinned host memory; every %dth request also every "
+                              "hit field" % SERVE_FULL_EVERY,
+                   "latency": "paced: scheduled arrival -> result in host memory; capacity: submission -> result",
+                   "server_config": {"served": "max_batch_requests 64, max_batch_rays 2^22, max_inflight 3",
+                                     "capacity_served": "max_batch_requests 64, max_batch_rays 2^25, max_inflight 3",
+                                     "serial_dispatch": "max_batch_requests 1, max_inflight 1 (one request per launch)"},
+                   "served": srv_, "serial_dispatch": sm["serial_dispatch"],
+                   "capacity_served": sm["capacity_served"], "capacity_serial_dispatch": sm["capacity_serial_dispatch"],
+                   "served_vs_serial": versus(sm["served"], sm["serial_dispatch"]),
+                   "capacity_vs_serial": versus(sm["capacity_served"], sm["capacity_serial_dispatch"]),
+                   "p50_ms": srv_["p50_ms"], "p99_ms": srv_["p99_ms"]},
         "roofline": None, "cpu_baseline": None,
-        "e2e": {"value": batched["value"], "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+        "e2e": {"value": srv_["value"], "unit": "Mrays/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": int(total_rays * 5 / n_req)},
-        "gpu_launches": batched["launches"], "clocks": clk,
-    }))
+        "gpu_launches": srv_["launches"][0] if srv_["launches"] else 0, "clocks": clk,
+        "parity": parity,
+    }
 
 
+# ---- f2 / f3 workloads --------------------------------------------------------------------------
 def viewport_rays(vp, W, H):
     """The rays of svo_render_viewport's pixels in image order (row 0 = top), formed on the host with
     examples/cpu_render.rs's f32 operations (the device forms the same bits)."""
@@ -678,8 +1169,7 @@ def run_viewport(args, w):
             scene.render_viewport(vp, W, H, img[k].data_ptr(), bad.data_ptr(), s)
 
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    clocks = ClockSampler(0)
-    clocks.start()
+    clocks = ClockSampler(0).start()
     for _ in range(args.warmup):
         render()
     torch.cuda.synchronize()
@@ -689,6 +1179,7 @@ def run_viewport(args, w):
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
+    frames = img.cpu().numpy()
     # end to end: the frames land in pinned host memory every step
     torch.cuda.synchronize()
     t1 = time.perf_counter()
@@ -734,10 +1225,9 @@ def run_viewport(args, w):
     o_all = np.concatenate([h[0] for h in host])
     d_all = np.concatenate([h[1] for h in host])
     cols = [np.ascontiguousarray(o_all[:, i]) for i in range(3)] + [np.ascontiguousarray(d_all[:, i]) for i in range(3)]
-    rays = {k: torch.from_numpy(c).to(dev) for k, c in zip(("ox", "oy", "oz", "dx", "dy", "dz"), cols)}
+    rays = {k: torch.from_numpy(c).to(dev) for k, c in zip(RAY_KEYS, cols)}
     rp = {k: v.data_ptr() for k, v in rays.items()}
-    tmap = {np.uint8: torch.uint8, np.uint32: torch.int32, np.float32: torch.float32}
-    outs = {k: torch.empty(n, dtype=tmap[svo.HIT_FIELDS[k]], device=dev) for k in ("status", "albedo", "nx", "ny", "nz")}
+    outs = device_outputs(torch, svo, n, dev, ("status", "albedo", "nx", "ny", "nz"))
     hp = {k: v.data_ptr() for k, v in outs.items()}
     for _ in range(args.warmup):
         scene.cast(rp, hp, n, s, row_length=W)
@@ -773,19 +1263,30 @@ def run_viewport(args, w):
     alg = alg_bytes_of(visits - runs, creads, vreads, hits) + 4 * n
     del cnt, rays, outs
 
-    cpu = None
-    if not args.no_cpu_baseline:
+    cpu, parity = None, None
+    if not args.no_parity:
         from oracle import oracle
         ot = oracle.Tree(w["size"], w["brick_dim"])
         ot.apply_ops(ops)
         threads = os.cpu_count() or 1
-        rate, m, stride, dt = cpu_cast_rate(ot, o_all, d_all, args.cpu_seconds, threads)
-        cpu = {"value": round(rate / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
-               "sample": "every %dth pixel ray of the 4 frames (%d rays, %.1fs on %d threads), cast only" % (
-                   stride, m, dt, threads)}
+        t0 = time.perf_counter()
+        ref_frames = []
+        bad_ref = 0
+        for vp in vps:
+            d = {"origin": list(vp.origin), "direction": list(vp.direction), "up": list(vp.up), "width": vp.width,
+                 "height": vp.height, "fov": vp.fov, "light": list(vp.light), "background": vp.background}
+            fr, b = ot.render_viewport(d, W, H, threads=threads)
+            ref_frames.append(fr)
+            bad_ref += b
+        cpu_s = time.perf_counter() - t0
+        mism = int(np.any(np.stack(ref_frames) != frames, axis=-1).sum())
+        parity = {"pixels_checked": n, "mismatches": mism, "unshaded_pixels_oracle": int(bad_ref),
+                  "what": "every RGBA8 pixel of the 4 frames against the oracle's restatement of cpu_render.rs"}
+        cpu = {"value": round(n / cpu_s / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": "the 4 frames rendered once (%.1fs on %d threads)" % (cpu_s, threads)}
     peak, peak_src = measured_peak()
     achieved = alg / (ms / 1e3) / 1e9
-    print(json.dumps({
+    return {
         "metric": "Mrays/s", "value": round(n / (ms / 1e3) / 1e6, 3), "unit": "Mrays/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -805,15 +1306,15 @@ def run_viewport(args, w):
                                                    "ms_per_step": round(cast_frames_ms, 4),
                                                    "note": "the same, one launch per frame like the render"}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": profile_traffic(args.workload).get("dram_bytes_per_launch"), "peak_source": peak_src,
-                     "alg_bytes_per_launch": alg, "alg_bytes_per_ray": round(alg / n, 2)},
+                     "frac": round(achieved / peak, 4), "traffic": profile_traffic("viewport512").get("dram_bytes_per_launch"),
+                     "peak_source": peak_src, "alg_bytes_per_launch": alg, "alg_bytes_per_ray": round(alg / n, 2)},
         "cpu_baseline": cpu,
         "e2e": {"value": round(n / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": n * 4,
                 "paths": {"one_launch_then_copy": round(n / e2e_one_s / 1e6, 3),
                           "two_streams_of_two_frames": round(n / e2e_pairs_s / 1e6, 3)}},
-        "gpu_launches": args.steps, "clocks": clk,
-    }))
+        "gpu_launches": args.steps, "clocks": clk, "parity": parity,
+    }
 
 
 def run_lod(args, w):
@@ -836,10 +1337,9 @@ def run_lod(args, w):
     origins, dirs = make_rays(svo, w)
     n = len(origins)
     cols = [np.ascontiguousarray(origins[:, i]) for i in range(3)] + [np.ascontiguousarray(dirs[:, i]) for i in range(3)]
-    rays = {k: torch.from_numpy(c).to(dev) for k, c in zip(("ox", "oy", "oz", "dx", "dy", "dz"), cols)}
+    rays = {k: torch.from_numpy(c).to(dev) for k, c in zip(RAY_KEYS, cols)}
     rp = {k: v.data_ptr() for k, v in rays.items()}
-    tmap = {np.uint8: torch.uint8, np.uint32: torch.int32, np.float32: torch.float32}
-    out = {k: torch.empty(n, dtype=tmap[svo.HIT_FIELDS[k]], device=dev) for k in OUT_FIELDS}
+    out = device_outputs(torch, svo, n, dev, OUT_FIELDS)
     hp = {k: v.data_ptr() for k, v in out.items()}
     vd = w["lod"]
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -856,15 +1356,15 @@ def run_lod(args, w):
         return e0.elapsed_time(e1) / args.steps
 
     row = ray_rows(w)  # camera images in raster order: svo_cast_lod_rows
-    clocks = ClockSampler(0)
-    clocks.start()
+    clocks = ClockSampler(0).start()
     ms = timed(lambda: scene.cast_lod(rp, hp, n, vd, s, row_length=row))
+    timed_out = host_fields(svo, out)
     max_ms = timed(lambda: scene.cast_lod(rp, hp, n, float(np.finfo(np.float32).max), s, row_length=row))
     plain_ms = timed(lambda: scene.cast(rp, hp, n, s, row_length=row))
     lod_plain_order_ms = timed(lambda: scene.cast_lod(rp, hp, n, vd, s))
     # end to end: rays from pinned host memory, status + albedo back, copies in the timed region
-    pin_in = {k: torch.from_numpy(c).pin_memory() for k, c in zip(("ox", "oy", "oz", "dx", "dy", "dz"), cols)}
-    pin_out = {k: torch.empty(n, dtype=tmap[svo.HIT_FIELDS[k]]).pin_memory() for k in ("status", "albedo")}
+    pin_in = {k: torch.from_numpy(c).pin_memory() for k, c in zip(RAY_KEYS, cols)}
+    pin_out = {k: torch.empty(n, dtype=out[k].dtype).pin_memory() for k in ("status", "albedo")}
 
     # one camera image per stream: its rays in, its LOD cast, its status and albedo out, so that one
     # image's copies overlap another's cast
@@ -906,20 +1406,23 @@ def run_lod(args, w):
     hits = int((st == 1).sum())
     mip_hits = int(((st == 1) & (oct_ == 8)).sum())
     alg = alg_bytes_of(visits - runs, creads, vreads, hits)
-    cpu = None
-    if not args.no_cpu_baseline:
+    cpu, parity = None, None
+    if not args.no_parity:
         from oracle import oracle
         ot = oracle.Tree(w["size"], w["brick_dim"])
         ot.apply_ops(ops)
         ot.mip_switch(True)
         threads = os.cpu_count() or 1
-        rate, m, step, dt = cpu_cast_rate(ot, origins, dirs, args.cpu_seconds, threads, viewing_distance=vd)
-        cpu = {"value": round(rate / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
-               "sample": "every %dth ray of the batch (%d rays, %.1fs on %d threads)" % (step, m, dt, threads)}
+        t0 = time.perf_counter()
+        ref = ot.cast(origins, dirs, threads=threads, viewing_distance=vd)
+        cpu_s = time.perf_counter() - t0
+        parity = merge_parity([compare_hits(timed_out, ref, "timed svo_cast_lod_rows launch")])
+        cpu = {"value": round(n / cpu_s / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": "the whole %d-ray batch, once (%.1fs on %d threads)" % (n, cpu_s, threads)}
     peak, peak_src = measured_peak()
     achieved = alg / (ms / 1e3) / 1e9
     st_ = scene.stats()
-    print(json.dumps({
+    return {
         "metric": "Mrays/s", "value": round(n / (ms / 1e3) / 1e6, 3), "unit": "Mrays/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -938,49 +1441,57 @@ def run_lod(args, w):
                    "svo_cast_lod_plain_order": {"value": round(n / (lod_plain_order_ms / 1e3) / 1e6, 3),
                                                 "ms_per_step": round(lod_plain_order_ms, 4)}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": profile_traffic(args.workload).get("dram_bytes_per_launch"), "peak_source": peak_src,
-                     "alg_bytes_per_launch": alg, "alg_bytes_per_ray": round(alg / n, 2)},
+                     "frac": round(achieved / peak, 4), "traffic": profile_traffic("lod512").get("dram_bytes_per_launch"),
+                     "peak_source": peak_src, "alg_bytes_per_launch": alg, "alg_bytes_per_ray": round(alg / n, 2)},
         "cpu_baseline": cpu,
         "e2e": {"value": round(n / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": n * 24,
                 "d2h_bytes_per_step": n * 5,
                 "how": "per camera image on its own stream: rays in, svo_cast_lod_rows, status + albedo out"},
-        "gpu_launches": args.steps, "clocks": clk,
-    }))
+        "gpu_launches": args.steps, "clocks": clk, "parity": parity,
+    }
+
+
+# ---- the reference arm: the oracle's CPU cast, no product code -----------------------------------
+def product_code_loaded():
+    """Whether this process has the product package imported or its library mapped."""
+    if any(m == "shocovox_gb300" or m.startswith("shocovox_gb300.") for m in sys.modules):
+        return True
+    try:
+        with open("/proc/self/maps") as f:
+            return "libsvo.so" in f.read()
+    except OSError:
+        return False
 
 
 def run_reference(args, w):
     rank, _, world = dist_env()
     if rank != 0:
         return
-    import shocovox_gb300 as svo
     from oracle import oracle
     t0 = time.perf_counter()
-    ops = scene_ops(svo, w)
+    ops = scene_ops(oracle, w)  # the oracle's own generators: the same ops and rays, no product code
     tree = oracle.Tree(w["size"], w["brick_dim"])
     tree.apply_ops(ops)
-    origins, dirs = make_rays(svo, w)
+    origins, dirs = make_rays(oracle, w)
     setup_s = time.perf_counter() - t0
     threads = os.cpu_count() or 1
     n = len(origins)
-    # calibrate a per-step sample of about 2 s of CPU work
-    rate, _, _, _ = cpu_cast_rate(tree, origins, dirs, 1.0, threads)
-    m = int(min(n, max(10000, rate * 2.0)))
-    stride = max(1, n // m)
-    so, sd = np.ascontiguousarray(origins[::stride]), np.ascontiguousarray(dirs[::stride])
     for _ in range(args.warmup):
-        tree.cast(so, sd, threads=threads)
+        tree.cast(origins, dirs, threads=threads)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        tree.cast(so, sd, threads=threads)
+        tree.cast(origins, dirs, threads=threads)
     dt = time.perf_counter() - t0
-    value = len(so) * args.steps / dt / 1e6
-    sample = "every %dth ray of the %d-ray batch (%d rays per step), oracle tree built in %.1fs" % (
-        stride, n, len(so), setup_s)
+    value = n * args.steps / dt / 1e6
+    sample = "the whole %d-ray batch every step (oracle scene, rays and tree built in %.1fs)" % (n, setup_s)
     print(json.dumps({
         "impl": "reference", "metric": "Mrays/s", "value": round(value, 4), "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "rays_per_step": len(so), "note": "CPU oracle cast, all host threads"},
+        "config": {"workload": args.workload, "rays_per_step": n, "voxels_inserted": int(len(ops)),
+                   "note": "CPU oracle cast (a restatement of the reference's get_by_ray; the Rust crate cannot be "
+                           "built here), all host threads, scene and rays from the oracle's generators",
+                   "product_code_loaded": product_code_loaded()},
         "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -994,192 +1505,49 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="terrain512", choices=sorted(WORKLOADS))
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle checks (and the CPU baseline)")
+    ap.add_argument("--no-north-star", action="store_true",
+                    help="skip the incoherent1024 / multiscene64 / served16 comparisons of the default run")
     ap.add_argument("--no-variants", action="store_true", help="skip the persistent-kernel autotune sweep")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
         if "multi" in w or "served" in w or "viewport" in w or "lod" in w:
-            print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the default single-scene workload"}))
+            print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the single-scene workloads "
+                                                                  "(terrain512, heightfield128, incoherent1024)"}))
             return
         run_reference(args, w)
         return
-    if "multi" in w:
-        run_multiscene(args, w)
-        return
-    if "served" in w:
-        run_served(args, w)
-        return
-    if "viewport" in w:
-        run_viewport(args, w)
-        return
-    if "lod" in w:
-        run_lod(args, w)
-        return
-
-    rank, local_rank, world = dist_env()
-    import torch
-    import shocovox_gb300 as svo
     pg = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("gloo")  # timing reduction only; the cast itself has no collective
-        pg = dist
-    torch.cuda.set_device(local_rank)
-    dev = torch.device("cuda", local_rank)
-
-    t0 = time.perf_counter()
-    ops = scene_ops(svo, w)
-    want_cpu = rank == 0 and not args.no_cpu_baseline
-    if want_cpu:
-        oth, obox = oracle_tree_async(ops, w)
-    scene = svo.Octree(w["size"], w["brick_dim"])
-    scene.apply_ops(ops)
-    build_s = time.perf_counter() - t0
-    stream = torch.cuda.current_stream(dev)
-    scene.upload(stream.cuda_stream)
-    origins, dirs = make_rays(svo, w)
-    n = len(origins)
-    cols_host = [np.ascontiguousarray(origins[:, i]) for i in range(3)] + [np.ascontiguousarray(dirs[:, i])
-                                                                          for i in range(3)]
-    rays_dev = {k: torch.from_numpy(c).to(dev) for k, c in zip(("ox", "oy", "oz", "dx", "dy", "dz"), cols_host)}
-    tmap = {np.uint8: torch.uint8, np.uint32: torch.int32, np.float32: torch.float32}
-    outs = {k: torch.empty(n, dtype=tmap[svo.HIT_FIELDS[k]], device=dev) for k in OUT_FIELDS}
-    rp = {k: v.data_ptr() for k, v in rays_dev.items()}
-    hp = {k: v.data_ptr() for k, v in outs.items()}
-    s = stream.cuda_stream
-
-    # camera rays in raster order: svo_cast_rows hands warps 8 x 4 blocks of neighbouring pixels
-    row = ray_rows(w)
-    clocks = ClockSampler(local_rank)
-    clocks.start()  # samples from the warm-up on, so that short timed regions still get samples
-    for _ in range(args.warmup):
-        scene.cast(rp, hp, n, s, row_length=row)
-    torch.cuda.synchronize()
-
-    # algorithmic bytes of one launch from the instrumented cast (counters equal the oracle's, see tests)
-    cnt = {k: torch.empty(n, dtype=torch.int32, device=dev) for k in COUNTERS}
-    st = torch.empty(n, dtype=torch.uint8, device=dev)
-    scene.cast(rp, dict(status=st.data_ptr(), **{k: v.data_ptr() for k, v in cnt.items()}), n, s, row_length=row)
-    torch.cuda.synchronize()
-    visits, creads, vreads, runs = (int(cnt[k].to(torch.int64).sum()) for k in COUNTERS)
-    hits = int((st == 1).sum())
-    alg_bytes = alg_bytes_of(visits - runs, creads, vreads, hits)
-    del cnt
-
-    if pg:
-        pg.barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        scene.cast(rp, hp, n, s, row_length=row)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    if pg:
-        pg.barrier()
-    ms = max_over_ranks(ms, pg)
-    ms_step = ms / args.steps
-    value = n * world / (ms_step / 1e3) / 1e6
-    # the same rays through plain svo_cast (warps take 32 consecutive rays of one row)
-    plain = None
-    if row:
-        if pg:
-            pg.barrier()
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(args.steps):
-            scene.cast(rp, hp, n, s)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        pms = max_over_ranks(e0.elapsed_time(e1), pg) / args.steps
-        plain = {"value": round(n * world / (pms / 1e3) / 1e6, 3), "ms_per_step": round(pms, 4)}
-
-    variants = None
-    if not args.no_variants:
-        variants = batched_variants(svo, torch, scene, rp, hp, n, stream, args, row)
-    clk = clocks.stop()
-
-    # end to end through the host-buffer C-ABI call (pinned host memory)
-    pin_cols = [torch.from_numpy(c).pin_memory() for c in cols_host]
-    pin_out = {k: torch.empty(n, dtype=tmap[svo.HIT_FIELDS[k]]).pin_memory() for k in OUT_FIELDS}
-    cols_np = [c.numpy() for c in pin_cols]
-    out_np = {k: v.numpy() for k, v in pin_out.items()}
-    for _ in range(max(1, args.warmup)):
-        scene.cast_host_soa(cols_np, out_np, s, row_length=row)
-    if pg:
-        pg.barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        scene.cast_host_soa(cols_np, out_np, s, row_length=row)
-    e2e_s = max_over_ranks(time.perf_counter() - t0, pg)
-    e2e_value = n * world * args.steps / e2e_s / 1e6
-    # the two ways svo_cast_host can move the data (svo_set_host_transfer), each timed the same way
-    e2e_paths = {}
-    for mode, name in ((1, "staged_copies"), (2, "direct_host_access")):
-        if svo.lib().svo_set_host_transfer(mode) != 0:
-            e2e_paths[name] = None
-            continue
-        scene.cast_host_soa(cols_np, out_np, s, row_length=row)
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            scene.cast_host_soa(cols_np, out_np, s, row_length=row)
-        e2e_paths[name] = round(n * world * args.steps / max_over_ranks(time.perf_counter() - t0, pg) / 1e6, 3)
-    svo.lib().svo_set_host_transfer(0)
-
-    cpu = None
-    if want_cpu:
-        oth.join()
-        tree = obox["tree"]
-        threads = os.cpu_count() or 1
-        rate, m, stride, dt = cpu_cast_rate(tree, origins, dirs, args.cpu_seconds, threads)
-        cpu = {"value": round(rate / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
-               "sample": "every %dth ray of the batch (%d rays, %.1fs on %d threads)" % (stride, m, dt, threads)}
-
-    peak, peak_src = measured_peak()
-    achieved = alg_bytes / (ms_step / 1e3) / 1e9
-    prof = profile_traffic(args.workload)
-    traffic = prof.get("dram_bytes_per_launch")
-    l2 = None
-    if prof.get("l2_bytes_per_launch"):
-        l2 = {"bytes_per_launch": prof["l2_bytes_per_launch"],
-              "gbs": round(prof["l2_bytes_per_launch"] / (ms_step / 1e3) / 1e9, 1),
-              "hit_rate_pct": prof.get("l2_hit_rate_pct"), "l1_hit_rate_pct": prof.get("l1_hit_rate_pct"),
-              "frac_of_l2_peak": round(prof["l2_throughput_pct_of_peak"] / 100.0, 4),
-              "source": "ncu capture of one launch (profiles/); gbs with this run's kernel time"}
+    if "multi" in w:
+        rec = run_multiscene(args, w)
+    elif "served" in w:
+        rec = run_served(args, w)
+    elif "viewport" in w:
+        rec = run_viewport(args, w)
+    elif "lod" in w:
+        rec = run_lod(args, w)
+    else:
+        rec, pg = run_single(args, w, args.workload)
+        _, _, world = dist_env()
+        if args.workload == "terrain512" and world == 1 and not args.no_north_star:
+            ns = {}
+            for name, fn in (("incoherent1024", lambda: north_star_incoherent(args)),
+                             ("multiscene64", lambda: run_multiscene(args, WORKLOADS["multiscene64"])),
+                             ("served16", lambda: run_served(args, WORKLOADS["served16"]))):
+                try:
+                    ns[name] = fn()
+                except Exception as e:  # recorded in the line (and fails the run), the other parts still report
+                    ns[name] = {"error": "%s: %s" % (type(e).__name__, e)}
+            rec["north_star"] = ns
+    rank, _, _ = dist_env()
     if rank == 0:
-        st = scene.stats()
-        print(json.dumps({
-            "metric": "Mrays/s", "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, "octree": "%d^3" % w["size"], "brick_dim": w["brick_dim"],
-                       "rays_per_step": n, "hit_rate": round(hits / n, 4), "nodes": st["nodes"],
-                       "per_ray": {"node_visits": round(visits / n, 2), "child_reads": round(creads / n, 2),
-                                   "voxel_reads": round(vreads / n, 2), "restart_run_visits": round(runs / n, 2)},
-                       "parted_bricks": st["parted_bricks"], "voxels_inserted": int(len(ops)),
-                       "l2": "inputs larger than L2 (rays %.0f MB + hits %.0f MB per step); the %.0f MB scene image "
-                             "stays resident" % (n * 24 / 1e6, n * sum(OUT_BYTES.values()) / 1e6,
-                                                 st["device_bytes"] / 1e6),
-                       "build_s": round(build_s, 1), "parallelism": "replicas" if world > 1 else "single",
-                       "ray_order": ("rows of %d rays (svo_cast_rows: 8 x 4 ray blocks per warp)" % row) if row
-                       else "as generated (svo_cast)",
-                       "svo_cast_plain_order": plain},
-            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_src,
-                         "alg_bytes_per_launch": alg_bytes,
-                         "alg_bytes_per_ray": round(alg_bytes / n, 2), "l2": l2},
-            "cpu_baseline": cpu,
-            "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": n * 24,
-                    "d2h_bytes_per_step": n * sum(OUT_BYTES.values()), "paths": e2e_paths},
-            "gpu_launches": args.steps,
-            "clocks": clk,
-            "variants": variants,
-        }))
+        print(json.dumps(rec))
     if pg:
         pg.destroy_process_group()
+    if parity_failed(rec):
+        sys.stderr.write("bench: a result differs from the oracle (see the parity records)\n")
+        sys.exit(1)
 
 
 if __name__ == "__main__":

@@ -110,7 +110,7 @@ const char* svo_last_error(void);
 int32_t svo_version(void);
 
 /* ---- construction and update (host) ---------------------------------- */
-/* Octree::new (src/octree/mod.rs:380-412) */
+/* Octree::new (src/octree/mod.rs:173-206) */
 svo_status svo_scene_create(uint32_t size, uint32_t brick_dim, svo_scene** out);
 void svo_scene_destroy(svo_scene* scene);
 /* Octree::auto_simplify (src/octree/types.rs:203) */
@@ -134,7 +134,7 @@ svo_status svo_apply_ops(svo_scene* scene, const svo_op* ops, uint64_t n, uint64
  * albedo (alpha 0) or user data (0) inserts nothing.  *n_done receives the number of inserts made. */
 svo_status svo_insert_dense(svo_scene* scene, uint32_t x0, uint32_t y0, uint32_t z0, uint32_t w, uint32_t h, uint32_t d,
                             const uint32_t* rgba, const uint32_t* user, uint64_t* n_done);
-/* Octree::get (src/octree/mod.rs:416-422) */
+/* Octree::get (src/octree/mod.rs:209-215) */
 svo_status svo_get(svo_scene* scene, uint32_t x, uint32_t y, uint32_t z, uint32_t* kind, uint32_t* rgba, uint32_t* user);
 svo_status svo_scene_stats_get(svo_scene* scene, svo_scene_stats* out);
 
@@ -149,7 +149,7 @@ svo_status svo_scene_save(svo_scene* scene, const char* path);
 svo_status svo_scene_load(const char* path, svo_scene** out);
 
 /* ---- MagicaVoxel .vox import (src/convert/magicavoxel.rs) -------------------------------- */
-/* Octree::load_vox_file (magicavoxel.rs:258-276): a new scene of size 2^ceil(log2(extent)) holding
+/* Octree::load_vox_file (magicavoxel.rs:266-286): a new scene of size 2^ceil(log2(extent)) holding
  * every voxel of frame 0 of the file's scene graph, inserted in file order as its palette colour. */
 svo_status svo_scene_from_vox(const uint8_t* bytes, uint64_t length, uint32_t brick_dim, svo_scene** out);
 svo_status svo_scene_load_vox(const char* path, uint32_t brick_dim, svo_scene** out);
@@ -295,7 +295,11 @@ typedef struct {
  * counts, a scatter into bucket order and a persistent cast of the sorted
  * entering rays, all on `stream`; the hits are the same as in index order.  The
  * sort's buffers grow only when the rays (or buckets) of a call outgrow them:
- * make the largest call once before a stream capture. */
+ * make the largest call once before a stream capture.  A graph that captured a
+ * call reads the workspace's host-side item table and device buffers at every
+ * replay: while that graph may still be replayed, make other casts through
+ * another workspace (a call on this one rewrites the table the graph reads,
+ * and one that outgrows the buffers frees those the graph uses). */
 typedef struct svo_batch_workspace svo_batch_workspace;
 svo_status svo_batch_workspace_create(svo_batch_workspace** out);
 void svo_batch_workspace_destroy(svo_batch_workspace* ws);
@@ -309,10 +313,14 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
  * scratch array compiled into the library (36,096 bytes, reserved on every GPU
  * that loads the library until the process exits), so at most 128 items are
  * accepted per call; more return SVO_ERR_ARGUMENT.  The first call on a device
- * looks up the array's device address (make it before any stream capture).
- * Calls that overlap on the GPU share the array and race: issue them on one
- * stream, or wait for one before starting the next.  Allocates nothing and
- * calls no allocating CUDA or library routine. */
+ * looks up the array's device address on the current device, which must be the
+ * device that owns `stream`; the address is kept for the life of the process,
+ * so a cudaDeviceReset makes it stale.  The item table is copied from the
+ * call's own stack frame, so a call on a stream that is being captured returns
+ * SVO_ERR_ARGUMENT with nothing enqueued.  Calls that overlap on the GPU share
+ * the array and race: issue them on one stream, or wait for one before
+ * starting the next.  Allocates nothing and calls no allocating CUDA or
+ * library routine. */
 svo_status svo_cast_batched_noalloc(const svo_batch_item* items, uint32_t n_items, const svo_launch_config* cfg,
                                     void* stream);
 

@@ -35,6 +35,14 @@ def viewport_struct(vp):
                     f3(*vp["light"]), vp["background"])
 
 
+class Recipe(ctypes.Structure):
+    """orc_recipe: a seeded synthetic scene (layout of the product's svo_scene_recipe)."""
+    _fields_ = [("kind", ctypes.c_uint32), ("size", ctypes.c_uint32), ("brick_dim", ctypes.c_uint32),
+                ("seed", ctypes.c_uint64), ("occupancy", ctypes.c_float), ("spheres", ctypes.c_uint32),
+                ("octaves", ctypes.c_uint32), ("base_freq", ctypes.c_float), ("height_lo", ctypes.c_float),
+                ("height_hi", ctypes.c_float), ("cave_threshold", ctypes.c_float)]
+
+
 class Hits(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in (
         "status", "brick_octant", "entry_kind", "node_key", "voxel_index", "pix", "albedo", "user",
@@ -53,7 +61,8 @@ def build(force=False):
     """Compiles the oracle with its Makefile (g++, no GPU needed)."""
     if force or not os.path.exists(_LIB_PATH) or \
             os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(os.path.join(_HERE, f))
-                                               for f in ("svo_oracle.cpp", "svo_oracle.h", "Makefile")):
+                                               for f in ("svo_oracle.cpp", "workloads.cpp", "svo_oracle.h",
+                                                         "Makefile")):
         subprocess.check_call(["make", "-s", "-C", _HERE])
     return _LIB_PATH
 
@@ -110,6 +119,12 @@ def lib():
         L.orc_stack_last.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
         L.orc_stack_add_last.argtypes = [vp, ctypes.c_int32]
         L.orc_stack_is_empty.argtypes = [vp]
+        fp = ctypes.POINTER(ctypes.c_float)
+        L.orc_gen_scene.argtypes = [ctypes.POINTER(Recipe), vp, u64, ctypes.POINTER(u64)]
+        L.orc_gen_camera_rays.argtypes = [fp, fp, ctypes.c_float, u32, u32, vp, vp, vp, vp, vp, vp]
+        L.orc_gen_camera_rays_strided.argtypes = [fp, fp, ctypes.c_float, u32, u32, u64, u64, u64, vp, vp, vp, vp, vp,
+                                                  vp]
+        L.orc_gen_sphere_rays.argtypes = [fp, ctypes.c_float, u64, u64, vp, vp, vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -345,3 +360,46 @@ class Stack:
 
     def is_empty(self):
         return bool(lib().orc_stack_is_empty(self._h))
+
+
+# ---- the benchmark's seeded workloads (workloads.cpp), with the product generators' signatures ----
+def gen_scene(kind, size, brick_dim, seed, occupancy=0.1, spheres=0, octaves=2, base_freq=1.0 / 32,
+              height_lo=0.0, height_hi=96.0, cave_threshold=0.55):
+    """Construction ops (OP_DTYPE) of a seeded synthetic scene."""
+    r = Recipe(kind, size, brick_dim, seed, occupancy, spheres, octaves, base_freq, height_lo, height_hi,
+               cave_threshold)
+    n = ctypes.c_uint64()
+    if lib().orc_gen_scene(ctypes.byref(r), None, 0, ctypes.byref(n)) != OK:
+        raise OracleError(ARGUMENT, "gen_scene")
+    ops = np.zeros(n.value, dtype=OP_DTYPE)
+    if lib().orc_gen_scene(ctypes.byref(r), _ptr(ops), n.value, ctypes.byref(n)) != OK:
+        raise OracleError(ARGUMENT, "gen_scene")
+    return ops
+
+
+def gen_camera_rays(eye, target, fov_deg, width, height):
+    """Pinhole camera rays in raster order: (origins (n,3), directions (n,3)) float32."""
+    cols = [np.zeros(width * height, dtype=np.float32) for _ in range(6)]
+    e, t = (ctypes.c_float * 3)(*eye), (ctypes.c_float * 3)(*target)
+    if lib().orc_gen_camera_rays(e, t, fov_deg, width, height, *[_ptr(c) for c in cols]) != OK:
+        raise OracleError(ARGUMENT, "gen_camera_rays")
+    return np.stack(cols[:3], axis=1), np.stack(cols[3:], axis=1)
+
+
+def gen_camera_rays_strided(eye, target, fov_deg, width, height, first, stride):
+    """The rays of pixels first, first + stride, ... of a camera image (raster order)."""
+    n = max(0, (width * height - first + stride - 1) // stride)
+    cols = [np.zeros(n, dtype=np.float32) for _ in range(6)]
+    e, t = (ctypes.c_float * 3)(*eye), (ctypes.c_float * 3)(*target)
+    if lib().orc_gen_camera_rays_strided(e, t, fov_deg, width, height, first, stride, n, *[_ptr(c) for c in cols]) != OK:
+        raise OracleError(ARGUMENT, "gen_camera_rays_strided")
+    return np.stack(cols[:3], axis=1), np.stack(cols[3:], axis=1)
+
+
+def gen_sphere_rays(center, radius, n, seed):
+    """Origins uniform on a sphere, directions uniform on S^2: (origins (n,3), directions (n,3)) float32."""
+    cols = [np.zeros(n, dtype=np.float32) for _ in range(6)]
+    c = (ctypes.c_float * 3)(*center)
+    if lib().orc_gen_sphere_rays(c, radius, n, seed, *[_ptr(a) for a in cols]) != OK:
+        raise OracleError(ARGUMENT, "gen_sphere_rays")
+    return np.stack(cols[:3], axis=1), np.stack(cols[3:], axis=1)

@@ -453,7 +453,7 @@ struct Entry {  // types.rs:23-36 OctreeEntry; kind bit0 = albedo, bit1 = data
   uint32_t user = 0;
 };
 static inline bool albedo_transparent(uint32_t rgba) { return (rgba & 0xFF) == 0; }  // detail.rs:70-72
-// octree/mod.rs:304-311 OctreeEntry::is_none
+// octree/mod.rs:97-104 OctreeEntry::is_none
 static bool entry_is_none(const Entry& e) {
   switch (e.kind) {
     case 0: return true;
@@ -537,7 +537,7 @@ struct Octree {
     return e;
   }
 
-  // ---------------- construction (octree/mod.rs:380-412) ----------------
+  // ---------------- construction (octree/mod.rs:173-206) ----------------
   static bool is_pow2(uint32_t v) { return v != 0 && (v & (v - 1)) == 0; }
   static int create(uint32_t size, uint32_t dim, Octree* t) {
     // `(x as f32).log(2.0).fract() != 0.0` checks are restated as exact power-of-two tests.
@@ -1464,7 +1464,7 @@ struct Octree {
   }
   static uint8_t child_octant_for(const Cube& b, V3f p) { return hash_region(p - b.min_position, b.size / 2.0f); }
 
-  // octree/mod.rs:416-578 (get = get_internal from the root)
+  // octree/mod.rs:209-371 (get = get_internal from the root)
   Entry get(const uint32_t upos[3]) { return get_internal(0, root_bounds((float)octree_size), upos); }
   Entry get_internal(size_t cur, Cube cb, const uint32_t upos[3]) {
     V3f position{(float)upos[0], (float)upos[1], (float)upos[2]};

@@ -128,6 +128,30 @@ void orc_child_bounds(const float cube[4], uint32_t octant, float out[4]);
 void orc_dda_step(const float ray[6], float point[3], const float cube[4], float step_out[3]);
 uint64_t orc_flat_projection(uint64_t x, uint64_t y, uint64_t z, uint64_t size);
 
+/* Seeded synthetic workloads of the benchmark (oracle/workloads.cpp): the same op lists and rays as
+   the product's svo_gen_scene / svo_gen_camera_rays / svo_gen_sphere_rays, so that the CPU baseline
+   needs no product code.  The recipe has the layout of svo_scene_recipe. */
+typedef struct {
+  uint32_t kind; /* 0 heightfield+spheres, 1 terrain+caves, 2 sparse+uniform blocks, 3 noise+spheres, 4 boxes */
+  uint32_t size, brick_dim;
+  uint64_t seed;
+  float occupancy;
+  uint32_t spheres;
+  uint32_t octaves;
+  float base_freq;
+  float height_lo, height_hi;
+  float cave_threshold;
+} orc_recipe;
+int orc_gen_scene(const orc_recipe* recipe, orc_op* ops, uint64_t max_ops, uint64_t* n_ops);
+int orc_gen_camera_rays(const float eye[3], const float target[3], float fov_deg, uint32_t width, uint32_t height,
+                        float* ox, float* oy, float* oz, float* dx, float* dy, float* dz);
+/* The camera rays of pixels first, first + stride, ... (n of them) of the width x height image. */
+int orc_gen_camera_rays_strided(const float eye[3], const float target[3], float fov_deg, uint32_t width,
+                                uint32_t height, uint64_t first, uint64_t stride, uint64_t n, float* ox, float* oy,
+                                float* oz, float* dx, float* dy, float* dz);
+int orc_gen_sphere_rays(const float center[3], float radius, uint64_t n, uint64_t seed, float* ox, float* oy, float* oz,
+                        float* dx, float* dy, float* dz);
+
 /* NodeStack<i32, size> harness for the ported ring-stack tests (size 1..8). */
 void* orc_stack_new(uint32_t size);
 void orc_stack_free(void* s);

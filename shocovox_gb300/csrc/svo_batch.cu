@@ -803,11 +803,20 @@ svo_status svo_cast_batched_noalloc(const svo_batch_item* items, uint32_t n_item
     return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: " + std::to_string(n_items) + " items exceed the maximum of " +
                                       std::to_string(kNoAllocMaxItems) + " per call");
   if (n_items == 0) return SVO_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  // The item table below is copied from this call's stack frame.  Inside a stream capture the copy
+  // would become a graph node that reads that frame again at every replay, long after it is gone, so
+  // a capturing stream is refused before anything is enqueued.
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  SVO_CUDA_TRY(cudaStreamIsCapturing(st, &capture));
+  if (capture != cudaStreamCaptureStatusNone)
+    return fail(SVO_ERR_ARGUMENT,
+                "svo_cast_batched_noalloc: the stream is capturing; its item table is copied from the caller's "
+                "stack and cannot be replayed (capture svo_cast_batched with a workspace instead)");
   void* scratch = nullptr;
   int sms = 0;
   svo_status rc = noalloc_scratch(&scratch, &sms);
   if (rc != SVO_OK) return rc;
-  cudaStream_t st = (cudaStream_t)stream;
   BatchItemDev table[kNoAllocMaxItems];
   const uint32_t shape = (cfg && cfg->block_shape) ? cfg->block_shape : 3;
   if (shape < 3 || shape > 5)

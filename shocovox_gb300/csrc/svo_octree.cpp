@@ -136,7 +136,7 @@ void BrickArena::release(uint32_t slot) {
 
 // ---------------------------------------------------------------- pool
 int HostOctree::create(uint32_t size, uint32_t dim, HostOctree* t) {
-  // Octree::new (src/octree/mod.rs:380-394); the f32 log2().fract() tests are exact power-of-two tests.
+  // Octree::new (src/octree/mod.rs:173-186); the f32 log2().fract() tests are exact power-of-two tests.
   auto pow2 = [](uint32_t v) { return v != 0 && (v & (v - 1)) == 0; };
   if (size == 0 || !pow2(dim)) return 2;
   if (dim > size || size % dim != 0 || !pow2(size / dim)) return 1;
@@ -144,7 +144,7 @@ int HostOctree::create(uint32_t size, uint32_t dim, HostOctree* t) {
   t->size = size;
   t->dim = dim;
   t->arena.init(dim);
-  t->push(Content{});  // root key 0 (mod.rs:397)
+  t->push(Content{});  // root key 0 (mod.rs:190)
   t->mips.assign(1, BrickRef{});  // node_mips: vec![BrickData::Empty] (mod.rs:198)
   // MIPMapStrategy::default (mipmap.rs:580-595)
   t->mip_methods = {{1, {kMipPoint, 0.0f}}, {2, {kMipBox, 0.0f}}, {3, {kMipBox, 0.0f}}, {4, {kMipBox, 0.0f}}};
@@ -1000,7 +1000,7 @@ int HostOctree::insert_at_lod(bool overwrite, const uint32_t up[3], uint32_t isz
   const Cube root{0.0f, 0.0f, 0.0f, (float)size};
   const float px = (float)up[0], py = (float)up[1], pz = (float)up[2];
   if (!contains(root, px, py, pz)) return 4;
-  bool none;  // OctreeEntry::is_none (src/octree/mod.rs:304-311)
+  bool none;  // OctreeEntry::is_none (src/octree/mod.rs:97-104)
   switch (data.kind & 3) {
     case 0: none = true; break;
     case 1: none = transparent(data.rgba); break;
@@ -1228,10 +1228,10 @@ int HostOctree::clear_at_lod(const uint32_t up[3], uint32_t csz) {
   return 0;
 }
 
-// ---------------------------------------------------------------- get (src/octree/mod.rs:416-578)
+// ---------------------------------------------------------------- get (src/octree/mod.rs:209-371)
 Entry HostOctree::get(const uint32_t up[3]) { return get_internal(0, Cube{0.0f, 0.0f, 0.0f, (float)size}, up); }
 
-// get_internal (mod.rs:219-300): the entry at a position within node k's bounds
+// get_internal (mod.rs:219-371): the entry at a position within node k's bounds
 Entry HostOctree::get_internal(size_t cur, Cube cb, const uint32_t up[3]) {
   const float px = (float)up[0], py = (float)up[1], pz = (float)up[2];
   if (!contains(cb, px, py, pz)) return Entry{};

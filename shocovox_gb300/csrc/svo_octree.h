@@ -86,7 +86,7 @@ struct Entry {
 
 class HostOctree {
  public:
-  // Octree::new (src/octree/mod.rs:380-412); returns an svo_status code.
+  // Octree::new (src/octree/mod.rs:173-206); returns an svo_status code.
   static int create(uint32_t size, uint32_t dim, HostOctree* t);
 
   int insert_at_lod(bool overwrite_if_empty, const uint32_t pos[3], uint32_t insert_size, const Entry& data);

@@ -205,9 +205,12 @@ void gen_dense(const svo_scene_recipe& r, OpSink& sink) {
   if (r.kind == 3) {
     std::vector<float> sample;
     Pcg32 gs(r.seed ^ 0xABCDull);
-    for (int i = 0; i < 8192; ++i)
-      sample.push_back(fbm3(gs.unit() * (float)S * r.base_freq, gs.unit() * (float)S * r.base_freq,
-                            gs.unit() * (float)S * r.base_freq, r.octaves ? r.octaves : 1, seed + 7u));
+    for (int i = 0; i < 8192; ++i) {
+      // drawn z, y, x: the order is spelled out so that every compiler makes the same sample
+      const float uz = gs.unit(), uy = gs.unit(), ux = gs.unit();
+      sample.push_back(fbm3(ux * (float)S * r.base_freq, uy * (float)S * r.base_freq, uz * (float)S * r.base_freq,
+                            r.octaves ? r.octaves : 1, seed + 7u));
+    }
     std::sort(sample.begin(), sample.end());
     size_t idx = (size_t)((1.0f - r.occupancy) * 8191.0f);
     thr = sample[idx < 8191 ? idx : 8191];

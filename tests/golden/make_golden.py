@@ -1,9 +1,10 @@
 """Extracts golden vectors from the reference crate's own source into JSON fixtures.
 
-Run in a checkout that has the reference mounted (it is not needed at test
-time; the fixtures are committed):
+Run with the root of a reference checkout as the argument, or in the
+SHOCOVOX_REFERENCE environment variable (it is not needed at test time; the
+fixtures are committed):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference checkout>
 
 Outputs
   tests/golden/luts.json      the constant look-up tables of src/spatial/lut.rs
@@ -90,7 +91,9 @@ def extract_rays(ref, relpath):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SHOCOVOX_REFERENCE", "")
+    if not ref or not os.path.isdir(os.path.join(ref, "src")):
+        sys.exit("usage: make_golden.py <reference checkout> (or set SHOCOVOX_REFERENCE)")
     here = os.path.dirname(os.path.abspath(__file__))
     with open(os.path.join(here, "luts.json"), "w") as f:
         json.dump(extract_luts(ref), f, indent=1)

@@ -305,7 +305,7 @@ def test_clear_to_nothing(backend):  # tests.rs:1198-1226
         assert t.get(o) == E
 
 
-def test_invalid_arguments(backend):  # octree/mod.rs:380-394 and insert.rs:106-114
+def test_invalid_arguments(backend):  # octree/mod.rs:173-186 and insert.rs:106-114
     from backends import creation_error
     assert creation_error(backend, 0, 1) == 2      # InvalidBrickDimension (size 0)
     assert creation_error(backend, 8, 3) == 2      # InvalidBrickDimension

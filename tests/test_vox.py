@@ -4,7 +4,8 @@ reference's own known answers: parse_rotation_matrix (magicavoxel.rs:387-414) an
 convert_coordinate (src/spatial/math/tests.rs:197-234).
 
 Scenes are written by tests/vox_writer.py; the reference's example models (assets/models/
-navigate*.vox) are imported too where the reference tree is present in this container."""
+navigate*.vox) are imported too where the SHOCOVOX_REFERENCE environment variable names a checkout
+of the reference."""
 import glob
 import os
 
@@ -16,7 +17,8 @@ from shocovox_gb300._lib import SvoError
 from oracle import vox as V
 from vox_writer import VALID_ROTATIONS, group, random_scene, shape, transform, vox_file
 
-ASSETS = sorted(glob.glob("/root/reference/assets/models/*.vox"))
+_REF = os.environ.get("SHOCOVOX_REFERENCE", "")
+ASSETS = sorted(glob.glob(os.path.join(_REF, "assets", "models", "*.vox"))) if _REF else []
 PANIC, ARGUMENT = 5, 6
 
 
