@@ -342,29 +342,34 @@ def batched_launches(items, sort_key):
     return (1 if claimed else 0) + (6 if sorted_items else 0)
 
 
-def sweep_batched(svo, torch, ws, items, stream, rows):
-    """Short autotune sweep of the batched cast on `items`: threads per block x rays per claim x ray-block
-    shape (items with a row length) or ray-sort key (items without).  Returns [(cfg tuple, ms)]."""
+def autotune_batched(svo, torch, ws, items, stream, fixed_sort=None):
+    """The project's autotuner (shocovox_gb300.autotune, no cache) on `items`: threads per block x rays
+    per claim x ray-block shape (items with a row length) or ray-sort key (items without), then the
+    staging depth of the best.  fixed_sort: only configurations with that sort key are kept.
+    Returns (LaunchConfig, {config string: ms})."""
+    from shocovox_gb300 import autotune
     s = stream.cuda_stream
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
-    def timed(cfg, reps):
+    def timed(cfg):
+        if fixed_sort is not None and cfg.sort_key != fixed_sort:
+            return float("inf")
         ws.cast(items, cfg, s)
         torch.cuda.synchronize()
         e0.record(stream)
-        for _ in range(reps):
+        for _ in range(2):
             ws.cast(items, cfg, s)
         e1.record(stream)
         torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / reps
+        return e0.elapsed_time(e1) / 2
 
-    sweep = []
-    for block in (64, 96, 128):
-        for chunk in (32, 64, 256):
-            for shape in ((3, 4) if rows else (0,)):
-                for sort in ((0,) if rows else (0, 1)):
-                    sweep.append(((block, chunk, shape, sort), timed(svo.LaunchConfig(block, chunk, 0, shape, sort), 2)))
-    return sweep
+    cfg, info = autotune.tune(ws, items, torch.cuda.get_device_name(0), timed, use_cache=False)
+    return cfg, {k: round(v, 4) for k, v in info["sweep_ms"].items() if v != float("inf")}
+
+
+def cfg_record(c):
+    return {"block": c.block, "rays_per_chunk": c.rays_per_chunk, "block_shape": c.block_shape, "sort_key": c.sort_key,
+            "staging_depth": c.staging_depth}
 
 
 # ---- single scene: terrain512 (default), heightfield128, incoherent1024 ----------------------------
@@ -458,17 +463,33 @@ def run_single(args, w, workload):
 
     variants = None
     if not args.no_variants:
+        # the plain cast with the top tree levels staged in shared memory (svo_set_staging_depth)
+        lib = svo.lib()
+
+        def staged(k):
+            def run():
+                lib.svo_set_staging_depth(k)
+                scene.cast(rp, hp, n, s, row_length=row)
+            return run
+        st_reps = interleaved_repeats({k: staged(k) for k in range(5)}, args.steps, 3, stream, torch)
+        lib.svo_set_staging_depth(0)
+        stage_sweep = {"depth%d" % k: spread(n * world, v) for k, v in st_reps.items()}
+        if want_check:
+            lib.svo_set_staging_depth(4)
+            scene.cast(rp, hp, n, s, row_length=row)
+            torch.cuda.synchronize()
+            lib.svo_set_staging_depth(0)
+            checks.append(("%s, staging depth 4" % ("svo_cast_rows" if row else "svo_cast"), host_fields(svo, outs)))
         ws = svo.BatchWorkspace()
         items = [(scene, rp, n, hp, row)]
-        sweep = sweep_batched(svo, torch, ws, items, stream, row)
-        (block, chunk, shape, sort), _ = min(sweep, key=lambda t: t[1])
-        cfg = svo.LaunchConfig(block, chunk, 0, shape, sort)
+        cfg, sweep = autotune_batched(svo, torch, ws, items, stream)
         bms = interleaved_repeats({"b": lambda: ws.cast(items, cfg, s)}, args.steps, 1, stream, torch)["b"][0]
-        variants = {"persistent_autotuned": {"value": round(n / (bms / 1e3) / 1e6, 3), "unit": "Mrays/s",
-                                             "ms_per_step": round(bms, 4), "block": block, "rays_per_chunk": chunk,
-                                             "block_shape": shape, "sort_key": sort,
-                                             "launches_per_step": batched_launches(items, sort)},
-                    "sweep_ms": {"%dx%dx%dx%d" % k: round(v, 3) for k, v in sweep}}
+        variants = {"persistent_autotuned": dict({"value": round(n / (bms / 1e3) / 1e6, 3), "unit": "Mrays/s",
+                                                  "ms_per_step": round(bms, 4),
+                                                  "launches_per_step": batched_launches(items, cfg.sort_key)},
+                                                 **cfg_record(cfg)),
+                    "sweep_ms": sweep,
+                    "plain_staging_depth_sweep": stage_sweep}
         if want_check:
             checks.append(("persistent batched kernel, autotuned", host_fields(svo, outs)))
     clk = clocks.stop()
@@ -592,11 +613,9 @@ def north_star_incoherent(args):
     hp = {v: {k: t.data_ptr() for k, t in o.items()} for v, o in outs.items()}
     ws = svo.BatchWorkspace()
     items = {v: [(scene, rp, n, hp[v], 0)] for v in ("index_order", "sorted")}
-    sweep = sweep_batched(svo, torch, ws, items["index_order"], stream, 0)
-    best = {}
+    best, sweeps = {}, {}
     for v, key in (("index_order", 0), ("sorted", 1)):
-        (b, c, sh, so), _ = min((t for t in sweep if t[0][3] == key), key=lambda t: t[1])
-        best[v] = svo.LaunchConfig(b, c, 0, sh, so)
+        best[v], sweeps[v] = autotune_batched(svo, torch, ws, items[v], stream, fixed_sort=key)
     clocks = ClockSampler(0).start()
     for _ in range(args.warmup):
         scene.cast(rp, hp["plain"], n, s)
@@ -615,9 +634,9 @@ def north_star_incoherent(args):
     res = {"svo_cast": plain}
     for v in ("index_order", "sorted"):
         c = best[v]
-        res["batched_" + v] = dict(spread(n, reps[v]), block=c.block, rays_per_chunk=c.rays_per_chunk,
-                                   sort_key=c.sort_key, launches_per_step=batched_launches(items[v], c.sort_key),
-                                   vs_plain=versus(spread(n, reps[v]), plain))
+        res["batched_" + v] = dict(spread(n, reps[v]), launches_per_step=batched_launches(items[v], c.sort_key),
+                                   vs_plain=versus(spread(n, reps[v]), plain), autotune_sweep_ms=sweeps[v],
+                                   **cfg_record(c))
     del outs, rays
     torch.cuda.empty_cache()
     return {"workload": "incoherent1024 (1024^3, brick 8, ~5% occupancy, 2^22 rays from the bounding sphere in "
@@ -755,11 +774,7 @@ def run_multiscene(args, w):
     torch.cuda.synchronize()
     checks.append(("one batched launch", host_fields(svo, dev_out)))
     # one persistent launch captured in a CUDA graph (workspace already sized, blocks per SM fixed)
-    if cfg.blocks_per_sm == 0:
-        per_sm = {64: 14, 96: 9, 128: 7}.get(cfg.block, 2)  # resident blocks at 72 registers per thread
-        gcfg = svo.LaunchConfig(cfg.block, cfg.rays_per_chunk, per_sm, cfg.block_shape, cfg.sort_key)
-    else:
-        gcfg = cfg
+    gcfg = cfg  # blocks per SM from occupancy when the call is captured, fixed in the graph
     gws = svo.BatchWorkspace()  # the graph keeps its own workspace: later casts on `ws` leave it alone
     gstream = torch.cuda.Stream(dev)
     graph = torch.cuda.CUDAGraph()
@@ -881,9 +896,7 @@ def run_multiscene(args, w):
                    "serial_plain": dict(serial_sp, launches_per_step=len(items)),
                    "batched": batched_sp,
                    "graph_vs_serial": versus(graph_sp, serial_sp),
-                   "autotune": {"block": cfg.block, "rays_per_chunk": cfg.rays_per_chunk, "block_shape": cfg.block_shape,
-                                "sort_key": cfg.sort_key, "cached": tune_info["cached"],
-                                "sweep_ms": tune_info.get("sweep_ms")}},
+                   "autotune": dict(cfg_record(cfg), cached=tune_info["cached"], sweep_ms=tune_info.get("sweep_ms"))},
         "roofline": {"bound": "hbm", "achieved": round(alg / (graph_ms / 1e3) / 1e9, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(alg / (graph_ms / 1e3) / 1e9 / peak, 4), "traffic": None, "peak_source": peak_src,
                      "alg_bytes_per_launch": alg, "alg_bytes_per_ray": round(alg / total, 2)},

@@ -285,6 +285,9 @@ typedef struct {
                               where the ray enters the octree), so that a warp's rays walk much the
                               same nodes (svo_cast_batched only: needs the workspace's buffers, which
                               grow to 128 bytes per such ray) */
+  uint32_t staging_depth;  /* top tree levels staged in shared memory by every block: the Internal nodes of
+                              depth < staging_depth (0..4) of each scene of the call, as far as 48 KB of
+                              records per block reach (scenes past that read their nodes from L1/L2) */
 } svo_launch_config;
 
 /* Casts every item's rays in one persistent kernel launch driven by a device
@@ -310,7 +313,7 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
  * device memory when they cast (a fixed memory budget handed over at start-up,
  * or a frame loop where a cudaMalloc would synchronise the device).  No
  * counterpart in the reference.  The item table and work counter live in one
- * scratch array compiled into the library (36,096 bytes, reserved on every GPU
+ * scratch array compiled into the library (47,360 bytes, reserved on every GPU
  * that loads the library until the process exits), so at most 128 items are
  * accepted per call; more return SVO_ERR_ARGUMENT.  The first call on a device
  * looks up the array's device address on the current device, which must be the
@@ -412,6 +415,13 @@ svo_status svo_set_cast_mode(int32_t mode);
  * copies otherwise; 1 always stages copies (chunks over three streams); 2 always accesses host
  * memory directly (an error where the device cannot). */
 svo_status svo_set_host_transfer(int32_t mode);
+/* Staging depth of the plain casts launched afterwards (svo_cast, svo_cast_rows and the host-buffer
+ * casts; process-wide): each block first copies the scene's Internal nodes of depth < depth (the
+ * root has depth 0; at most 1, 9, 73 or 585 records of 64 bytes for depth 1..4) into shared memory,
+ * and the traversal reads those nodes there instead of through L1/L2.  0 (default) stages nothing.
+ * The results are the same at every depth; the batched cast takes its depth from
+ * svo_launch_config.staging_depth.  No counterpart in the reference. */
+svo_status svo_set_staging_depth(int32_t depth);
 
 #ifdef __cplusplus
 }

@@ -54,7 +54,7 @@ class SceneRecipe(ctypes.Structure):
 
 class LaunchConfig(ctypes.Structure):
     _fields_ = [("block", ctypes.c_uint32), ("rays_per_chunk", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32),
-                ("block_shape", ctypes.c_uint32), ("sort_key", ctypes.c_uint32)]
+                ("block_shape", ctypes.c_uint32), ("sort_key", ctypes.c_uint32), ("staging_depth", ctypes.c_uint32)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -145,6 +145,7 @@ SIGNATURES = {
     "svo_selftest_luts": (_I32, [_P(_U64), _P(_U32), _P(_U64)]),
     "svo_set_cast_mode": (_I32, [_I32]),
     "svo_set_host_transfer": (_I32, [_I32]),
+    "svo_set_staging_depth": (_I32, [_I32]),
 }
 
 

@@ -30,7 +30,52 @@ struct BatchItemDev {
   ClaimOrder order;  // the item's rays by claim and lane
   uint64_t begin;    // first global index of the item (a multiple of 32)
   uint64_t n;
+  const DevNode* stage_src;  // the first item of each staged scene: its top table, which blocks copy
+  uint32_t stage_off;        // the scene's staged records in the block's copy: [stage_off, + stage_n)
+  uint32_t stage_n;          // 0: the scene's nodes are read from L1/L2
 };
+
+constexpr uint32_t kBatchStageRecords = 768;  // 48 KB of staged records per block at most
+
+// Shares the staged records out among the scenes of a call, in order of first appearance, at staging
+// depth `depth` while they fit kBatchStageRecords; returns the records a block copies.
+inline uint32_t assign_staging(BatchItemDev* table, const svo_batch_item* items, uint32_t n_items, uint32_t depth) {
+  uint32_t total = 0;
+  for (uint32_t i = 0; i < n_items; ++i) {
+    table[i].stage_src = nullptr;
+    table[i].stage_off = 0;
+    table[i].stage_n = 0;
+  }
+  if (depth == 0) return 0;
+  for (uint32_t i = 0; i < n_items; ++i) {
+    uint32_t first = i;
+    for (uint32_t j = 0; j < i; ++j)
+      if (items[j].scene == items[i].scene) {
+        first = j;
+        break;
+      }
+    if (first < i) {  // a later item of a scene seen before: the same staged records
+      table[i].stage_off = table[first].stage_off;
+      table[i].stage_n = table[first].stage_n;
+      continue;
+    }
+    const uint32_t n = table[i].scene.literal ? 0u : staged_records(items[i].scene, depth);
+    if (n == 0 || total + n > kBatchStageRecords) continue;
+    table[i].stage_src = table[i].scene.top;
+    table[i].stage_off = total;
+    table[i].stage_n = n;
+    total += n;
+  }
+  return total;
+}
+
+// The staged records of every scene of the table into the block's shared-memory copy.
+__device__ __forceinline__ void stage_items(DevNode* stg, const BatchItemDev* items, uint32_t n_items) {
+  for (uint32_t i = 0; i < n_items; ++i) {
+    const DevNode* src = items[i].stage_src;
+    if (src) stage_records(stg + items[i].stage_off, src, items[i].stage_n);
+  }
+}
 
 // fills the device form of one item at global index `begin`; returns the indices it spans
 // (none when the item's rays are cast through the ray sort instead: `claimed` false)
@@ -61,16 +106,19 @@ struct WaitingBatchRays {
   unsigned long long i[64];
 };
 
-template <bool kCount>
+template <bool kCount, bool kStage = false>
 __global__ void __launch_bounds__(kBatchMaxBlock, 7)
     batched_kernel(const BatchItemDev* __restrict__ items, uint32_t n_items, uint64_t total,
                    unsigned long long* __restrict__ counter, uint32_t chunk) {
   __shared__ uint64_t s_begin[kMaxSharedItems];
   __shared__ SharedLuts L;
   __shared__ WaitingBatchRays waiting[kBatchMaxBlock / 32];
+  extern __shared__ uint4 staged_smem[];
+  DevNode* stg = reinterpret_cast<DevNode*>(staged_smem);
   const uint32_t staged = n_items < kMaxSharedItems ? n_items : kMaxSharedItems;
   for (uint32_t i = threadIdx.x; i < staged; i += blockDim.x) s_begin[i] = items[i].begin;
   fill_shared_luts(L);
+  if (kStage) stage_items(stg, items, n_items);
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31u;
   WaitingBatchRays& w = waiting[threadIdx.x >> 5];
@@ -180,7 +228,8 @@ __global__ void __launch_bounds__(kBatchMaxBlock, 7)
       dz = __ldg(r.dz + i);
     }
     HitRecord h;
-    cast_entered<kCount>(it.scene, L, ox, oy, oz, dx, dy, dz, fast, px, py, pz, target, h);
+    cast_entered<kCount, false, kStage>(it.scene, L, ox, oy, oz, dx, dy, dz, fast, px, py, pz, target, h, 0.0f,
+                                        stg + it.stage_off, it.stage_n);
     write_hit(it.scene, it.hits, i, h);
     if (kCount) write_counters(it.hits, i, h);
   }
@@ -493,13 +542,22 @@ __global__ void __launch_bounds__(kSortBlock)
   }
 }
 
-template <bool kCount, bool kOne>
+template <bool kCount, bool kOne, bool kStage = false>
 __global__ void __launch_bounds__(kBatchMaxBlock, 7)
     sorted_cast_kernel(const BatchItemDev* __restrict__ items, const SortedRay* __restrict__ sorted,
                        const unsigned long long* __restrict__ n_list, unsigned long long* __restrict__ counter,
-                       uint32_t chunk, const SceneView one_scene, const HitsView one_hits) {
+                       uint32_t chunk, const SceneView one_scene, const HitsView one_hits, uint32_t n_items,
+                       uint32_t one_stage_n) {
   __shared__ SharedLuts L;
+  extern __shared__ uint4 staged_smem[];
+  DevNode* stg = reinterpret_cast<DevNode*>(staged_smem);
   fill_shared_luts(L);
+  if (kStage) {
+    if (kOne)
+      stage_records(stg, one_scene.top, one_stage_n);
+    else
+      stage_items(stg, items, n_items);
+  }
   __syncthreads();
   const uint64_t n = *n_list;
   const uint32_t lane = threadIdx.x & 31u;
@@ -518,12 +576,14 @@ __global__ void __launch_bounds__(kBatchMaxBlock, 7)
       const bool fast = (target >> 31) != 0u;
       HitRecord h;
       if (kOne) {
-        cast_entered<kCount>(one_scene, L, a.x, a.y, a.z, a.w, b.x, b.y, fast, b.z, b.w, c.x, target & 0x7FFFFFFFu, h);
+        cast_entered<kCount, false, kStage>(one_scene, L, a.x, a.y, a.z, a.w, b.x, b.y, fast, b.z, b.w, c.x,
+                                            target & 0x7FFFFFFFu, h, 0.0f, stg, one_stage_n);
         write_hit(one_scene, one_hits, i, h);
         if (kCount) write_counters(one_hits, i, h);
       } else {
         const BatchItemDev& it = items[__float_as_uint(c.z)];
-        cast_entered<kCount>(it.scene, L, a.x, a.y, a.z, a.w, b.x, b.y, fast, b.z, b.w, c.x, target & 0x7FFFFFFFu, h);
+        cast_entered<kCount, false, kStage>(it.scene, L, a.x, a.y, a.z, a.w, b.x, b.y, fast, b.z, b.w, c.x,
+                                            target & 0x7FFFFFFFu, h, 0.0f, stg + it.stage_off, it.stage_n);
         write_hit(it.scene, it.hits, i, h);
         if (kCount) write_counters(it.hits, i, h);
       }
@@ -531,6 +591,31 @@ __global__ void __launch_bounds__(kBatchMaxBlock, 7)
   }
 }
 
+}  // namespace svo
+
+namespace svo {
+// The claim-order persistent launch of a prepared item table (device copy at d_items), with
+// staged_n records of the call's top tables staged by every block.
+svo_status launch_claimed(const BatchItemDev* d_items, uint32_t n_items, uint64_t total,
+                          unsigned long long* d_counter, uint32_t chunk, uint32_t block, const svo_launch_config* cfg,
+                          bool count, uint32_t staged_n, int sm_count, cudaStream_t st) {
+  const size_t smem = (size_t)staged_n * sizeof(DevNode);
+  auto kern = staged_n ? (count ? batched_kernel<true, true> : batched_kernel<false, true>)
+                       : (count ? batched_kernel<true> : batched_kernel<false>);
+  int per_sm = (cfg && cfg->blocks_per_sm) ? (int)cfg->blocks_per_sm : 0;
+  if (per_sm == 0) {
+    SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem));
+    per_sm = std::max(per_sm, 1);
+  }
+  const uint64_t warps_needed = (total + chunk - 1) / chunk;
+  uint64_t grid = (uint64_t)sm_count * (uint64_t)per_sm;
+  grid = std::min<uint64_t>(grid, (warps_needed * 32 + block - 1) / block);
+  grid = std::max<uint64_t>(grid, 1);
+  SVO_CUDA_TRY(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st));
+  kern<<<(unsigned)grid, block, smem, st>>>(d_items, n_items, total, d_counter, chunk);
+  SVO_CUDA_TRY(cudaGetLastError());
+  return SVO_OK;
+}
 }  // namespace svo
 
 // Workspace of the batched cast: device item table + work counter, and a
@@ -649,6 +734,11 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
   if (total == 0 && sort_total == 0) return SVO_OK;
   if (sort_total >= (1ull << 32) || buckets >= (1ull << 32))
     return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: the ray sort takes fewer than 2^32 rays per call");
+  const uint32_t depth = cfg ? cfg->staging_depth : 0;
+  if (depth > kMaxStageDepth)
+    return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: staging_depth must be 0.." + std::to_string(kMaxStageDepth));
+  const uint32_t staged_n = assign_staging(ws->h_items, items, n_items, depth);
+  const size_t stage_smem = (size_t)staged_n * sizeof(DevNode);
   const uint32_t block = (cfg && cfg->block) ? cfg->block : 128;
   const uint32_t chunk = (cfg && cfg->rays_per_chunk) ? cfg->rays_per_chunk : 64;
   if (block % 32 != 0 || block > kBatchMaxBlock || chunk == 0)
@@ -715,39 +805,28 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
     scan_top<<<1, 1024, 0, st>>>(ws->d_sums, tiles);
     scan_down<<<tiles, kSortBlock, 0, st>>>(ws->d_hist, buckets, ws->d_sums);
     scatter_kernel<<<bin_grid, kSortBlock, 0, st>>>(ws->d_list, n_list, ws->d_hist, ws->d_sorted);
-    auto cast = single ? (count ? sorted_cast_kernel<true, true> : sorted_cast_kernel<false, true>)
-                       : (count ? sorted_cast_kernel<true, false> : sorted_cast_kernel<false, false>);
+    // the one sorted item's staged records sit at the start of the block's copy
+    const uint32_t one_stage = single ? ws->h_items[one.index].stage_n : 0u;
+    const bool stage = single ? one_stage > 0 : staged_n > 0;
+    const size_t smem = single ? (size_t)one_stage * sizeof(DevNode) : stage_smem;
+    auto cast = stage ? (single ? (count ? sorted_cast_kernel<true, true, true> : sorted_cast_kernel<false, true, true>)
+                                : (count ? sorted_cast_kernel<true, false, true> : sorted_cast_kernel<false, false, true>))
+                      : (single ? (count ? sorted_cast_kernel<true, true> : sorted_cast_kernel<false, true>)
+                                : (count ? sorted_cast_kernel<true, false> : sorted_cast_kernel<false, false>));
     int per_sm = (cfg && cfg->blocks_per_sm) ? (int)cfg->blocks_per_sm : 0;
     if (per_sm == 0) {
-      SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cast, block, 0));
+      SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cast, block, smem));
       per_sm = std::max(per_sm, 1);
     }
     const uint64_t warps_needed = (sort_total + chunk - 1) / chunk;
     uint64_t grid = (uint64_t)ws->sm_count * (uint64_t)per_sm;
     grid = std::max<uint64_t>(1, std::min<uint64_t>(grid, (warps_needed * 32 + block - 1) / block));
-    cast<<<(unsigned)grid, block, 0, st>>>(ws->d_items, ws->d_sorted, n_list, ws->d_counter, chunk, one.scene, one.hits);
+    cast<<<(unsigned)grid, block, smem, st>>>(ws->d_items, ws->d_sorted, n_list, ws->d_counter, chunk, one.scene,
+                                               one.hits, n_items, one_stage);
     SVO_CUDA_TRY(cudaGetLastError());
   }
   if (total == 0) return SVO_OK;
-  int per_sm = (cfg && cfg->blocks_per_sm) ? (int)cfg->blocks_per_sm : 0;
-  if (per_sm == 0) {
-    if (count)
-      SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_kernel<true>, block, 0));
-    else
-      SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_kernel<false>, block, 0));
-    per_sm = std::max(per_sm, 1);
-  }
-  const uint64_t warps_needed = (total + chunk - 1) / chunk;
-  uint64_t grid = (uint64_t)ws->sm_count * (uint64_t)per_sm;
-  grid = std::min<uint64_t>(grid, (warps_needed * 32 + block - 1) / block);
-  grid = std::max<uint64_t>(grid, 1);
-  SVO_CUDA_TRY(cudaMemsetAsync(ws->d_counter, 0, sizeof(unsigned long long), st));
-  if (count)
-    batched_kernel<true><<<(unsigned)grid, block, 0, st>>>(ws->d_items, n_items, total, ws->d_counter, chunk);
-  else
-    batched_kernel<false><<<(unsigned)grid, block, 0, st>>>(ws->d_items, n_items, total, ws->d_counter, chunk);
-  SVO_CUDA_TRY(cudaGetLastError());
-  return SVO_OK;
+  return launch_claimed(ws->d_items, n_items, total, ws->d_counter, chunk, block, cfg, count, staged_n, ws->sm_count, st);
 }
 
 }  // extern "C"
@@ -766,6 +845,7 @@ constexpr uint32_t kNoAllocMaxItems = 128;  // items per call
 constexpr size_t kNoAllocTableBytes = kNoAllocMaxItems * sizeof(svo::BatchItemDev);
 constexpr size_t kNoAllocCounterOffset = (kNoAllocTableBytes + 255) / 256 * 256;
 constexpr size_t kNoAllocBytes = kNoAllocCounterOffset + 256;
+static_assert(kNoAllocBytes == 47360, "include/svo.h documents the scratch array's size");
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 namespace {
@@ -839,31 +919,17 @@ svo_status svo_cast_batched_noalloc(const svo_batch_item* items, uint32_t n_item
   const uint32_t chunk = (cfg && cfg->rays_per_chunk) ? cfg->rays_per_chunk : 64;
   if (block % 32 != 0 || block > kBatchMaxBlock || chunk == 0)
     return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: block must be a multiple of 32 and at most 128");
-  int per_sm = (cfg && cfg->blocks_per_sm) ? (int)cfg->blocks_per_sm : 0;
-  if (per_sm == 0) {
-    if (count)
-      SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_kernel<true>, block, 0));
-    else
-      SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_kernel<false>, block, 0));
-    per_sm = std::max(per_sm, 1);
-  }
-  const uint64_t warps_needed = (total + chunk - 1) / chunk;
-  uint64_t grid = (uint64_t)sms * (uint64_t)per_sm;
-  grid = std::min<uint64_t>(grid, (warps_needed * 32 + block - 1) / block);
-  grid = std::max<uint64_t>(grid, 1);
+  const uint32_t depth = cfg ? cfg->staging_depth : 0;
+  if (depth > kMaxStageDepth)
+    return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: staging_depth must be 0.." + std::to_string(kMaxStageDepth));
+  const uint32_t staged_n = assign_staging(table, items, n_items, depth);
   BatchItemDev* d_items = static_cast<BatchItemDev*>(scratch);
   unsigned long long* d_counter =
       reinterpret_cast<unsigned long long*>(static_cast<unsigned char*>(scratch) + kNoAllocCounterOffset);
-  // the table is copied from this stack frame: a pageable source is staged before cudaMemcpyAsync returns
+  // the table is copied from this stack frame: a pageable source is staged before cudaMemcpyAsync returns;
+  // the counter keeps the previous call's final value and is reset for this launch by launch_claimed
   SVO_CUDA_TRY(cudaMemcpyAsync(d_items, table, n_items * sizeof(BatchItemDev), cudaMemcpyHostToDevice, st));
-  // the counter keeps the previous call's final value: reset it for this launch
-  SVO_CUDA_TRY(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st));
-  if (count)
-    batched_kernel<true><<<(unsigned)grid, block, 0, st>>>(d_items, n_items, total, d_counter, chunk);
-  else
-    batched_kernel<false><<<(unsigned)grid, block, 0, st>>>(d_items, n_items, total, d_counter, chunk);
-  SVO_CUDA_TRY(cudaGetLastError());
-  return SVO_OK;
+  return launch_claimed(d_items, n_items, total, d_counter, chunk, block, cfg, count, staged_n, sms, st);
 }
 
 }  // extern "C"

@@ -669,10 +669,14 @@ __device__ __forceinline__ bool fast_entry(const SceneView& s, float ox, float o
 }
 
 // The fast form's traversal of a ray that entered the root at (px, py, pz), in its octant `target`.
-template <bool kCount, bool kLod = false>
+// kStage: the first stg_n records of the scene's top table are staged at `stg` (shared memory); a
+// node key with kStagedBit set names one of them.  Only Internal nodes are staged, so the key of a
+// node that holds a hit never carries the bit.
+template <bool kCount, bool kLod = false, bool kStage = false>
 __device__ void cast_ray_fast_from(const SceneView& s, const SharedLuts& L, float ox, float oy, float oz, float dx,
                                    float dy, float dz, float px, float py, float pz, uint32_t target, HitRecord& h,
-                                   float viewing_distance = 0.0f) {
+                                   float viewing_distance = 0.0f, const DevNode* stg = nullptr, uint32_t stg_n = 0) {
+  static_assert(!(kStage && kLod), "a MIP hit reports its node's key: the LOD cast reads no staged copy");
   miss_record(h);
   FastRay r;
   r.dx = dx;
@@ -698,10 +702,11 @@ __device__ void cast_ray_fast_from(const SceneView& s, const SharedLuts& L, floa
   uint32_t work = 0;
   float mip_level = s.mip_top;  // (:350) kept across restarts
   const bool lod = kLod && s.mips;
+  const uint32_t root = (kStage && stg_n) ? kStagedBit : 0u;
   while (target != kOob) {
-    uint32_t cur = 0;
+    uint32_t cur = root;
     cb = Bounds{0.0f, 0.0f, 0.0f, S, s.inv_size};
-    uint32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0, count = 1;
+    uint32_t s0 = root, s1 = 0, s2 = 0, s3 = 0, count = 1;
     uint32_t oct = 0;  // octant of each stack entry in its parent, newest in the low 3 bits
     while (count > 0) {
       if (++work > kWorkCap) {
@@ -709,8 +714,10 @@ __device__ void cast_ray_fast_from(const SceneView& s, const SharedLuts& L, floa
         return;
       }
       if (kCount) h.visits++;
+      const bool staged = kStage && (cur & kStagedBit) != 0u;
       const DevNode* nd = s.nodes + cur;
-      const uint4 head = __ldg(reinterpret_cast<const uint4*>(nd));
+      const DevNode* sn = kStage ? stg + (cur & ~kStagedBit) : nd;
+      const uint4 head = staged ? *reinterpret_cast<const uint4*>(sn) : __ldg(reinterpret_cast<const uint4*>(nd));
       const uint64_t occ = ((uint64_t)head.y << 32) | head.x;
       const uint32_t meta = head.z;
       const uint32_t kind = meta & 3u;
@@ -770,10 +777,15 @@ __device__ void cast_ray_fast_from(const SceneView& s, const SharedLuts& L, floa
         continue;
       }
       Bounds tb = child_bounds(cb, target);
-      uint32_t ck = kind == kKindInternal ? __ldg(&nd->slot[target]) : kInvalidChild;
+      uint32_t ck = kind == kKindInternal ? (staged ? sn->slot[target] : __ldg(&nd->slot[target])) : kInvalidChild;
       if (kCount) h.creads++;
       if (ck != kInvalidChild && (occ & L.octant[target]) != 0) {
-        // PUSH (the child's octant in its parent rides along: 3 bits per stack entry)
+        // PUSH (the child's octant in its parent rides along: 3 bits per stack entry); a staged
+        // node's staged child is entered through its copy
+        if (staged) {
+          const uint32_t si = sn->stage[target];
+          if (si < stg_n) ck = kStagedBit | si;
+        }
         oct = ((oct << 3) | target) & 0xFFFu;
         cur = ck;
         cb = tb;
@@ -799,7 +811,7 @@ __device__ void cast_ray_fast_from(const SceneView& s, const SharedLuts& L, floa
           target = step_fast(target, move, r.pos);
           if (target == kOob) break;
           tb = child_bounds(cb, target);
-          ck = kind == kKindInternal ? __ldg(&nd->slot[target]) : kInvalidChild;
+          ck = kind == kKindInternal ? (staged ? sn->slot[target] : __ldg(&nd->slot[target])) : kInvalidChild;
           if (kCount) h.creads++;
           if (move & 1u) bx = bx + dbx;
           if (move & 4u) by = by + dby;
@@ -921,13 +933,16 @@ __device__ __noinline__ void cast_ray_literal_lod(const SceneView& s, const Shar
 }
 
 // cast_one for a ray whose way in is known: `fast` with its fast_entry (px, py, pz, target), else the
-// literal form (a NaN in the direction, or literal mode).
-template <bool kCount, bool kLod = false>
+// literal form (a NaN in the direction, or literal mode).  kStage: the fast form reads the first stg_n
+// top-table records from their copy at `stg` (shared memory).
+template <bool kCount, bool kLod = false, bool kStage = false>
 __device__ __forceinline__ void cast_entered(const SceneView& s, const SharedLuts& L, float ox, float oy, float oz,
                                              float dx, float dy, float dz, bool fast, float px, float py, float pz,
-                                             uint32_t target, HitRecord& h, float viewing_distance = 0.0f) {
+                                             uint32_t target, HitRecord& h, float viewing_distance = 0.0f,
+                                             const DevNode* stg = nullptr, uint32_t stg_n = 0) {
   if (fast)
-    cast_ray_fast_from<kCount, kLod>(s, L, ox, oy, oz, dx, dy, dz, px, py, pz, target, h, viewing_distance);
+    cast_ray_fast_from<kCount, kLod, kStage>(s, L, ox, oy, oz, dx, dy, dz, px, py, pz, target, h, viewing_distance,
+                                             stg, stg_n);
   else if (kLod)
     cast_ray_literal_lod<kCount>(s, L, ox, oy, oz, dx, dy, dz, h, viewing_distance);
   else
@@ -1039,5 +1054,13 @@ __device__ __forceinline__ void write_counters(const HitsView& o, uint64_t i, co
 struct RaysView {
   const float *ox, *oy, *oz, *dx, *dy, *dz;
 };
+
+// Copies `n` top-table records from `src` (global) to `dst` (shared memory) with the block's threads,
+// 16 bytes per load.  The caller synchronises the block before the copy is read.
+__device__ __forceinline__ void stage_records(DevNode* dst, const DevNode* src, uint32_t n) {
+  const uint4* a = reinterpret_cast<const uint4*>(src);
+  uint4* b = reinterpret_cast<uint4*>(dst);
+  for (uint32_t i = threadIdx.x; i < n * (uint32_t)(sizeof(DevNode) / 16); i += blockDim.x) b[i] = __ldg(a + i);
+}
 
 }  // namespace svo

@@ -46,13 +46,18 @@ struct WaitingRays {  // the ray's origin and direction are read again from the 
   unsigned long long i[64];
 };
 
-template <bool kCount, bool kLod = false>
+// kStage: the block first copies the scene's top table's first stage_n records into dynamic shared
+// memory, and the fast form reads those nodes there.
+template <bool kCount, bool kLod = false, bool kStage = false>
 __global__ void __launch_bounds__(128, 7)
     queue_kernel(SceneView s, RaysView rays, HitsView out, uint64_t n, ClaimOrder order,
-                 unsigned long long* __restrict__ counter, float viewing_distance = 0.0f) {
+                 unsigned long long* __restrict__ counter, float viewing_distance = 0.0f, uint32_t stage_n = 0) {
   __shared__ SharedLuts L;
   __shared__ WaitingRays waiting[4];
+  extern __shared__ uint4 staged_smem[];
+  DevNode* stg = reinterpret_cast<DevNode*>(staged_smem);
   fill_shared_luts(L);
+  if (kStage) stage_records(stg, s.top, stage_n);
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31u;
   WaitingRays& w = waiting[threadIdx.x >> 5];
@@ -130,7 +135,8 @@ __global__ void __launch_bounds__(128, 7)
     }
     if (!have) continue;
     HitRecord h;
-    cast_entered<kCount, kLod>(s, L, ox, oy, oz, dx, dy, dz, fast, px, py, pz, target, h, viewing_distance);
+    cast_entered<kCount, kLod, kStage>(s, L, ox, oy, oz, dx, dy, dz, fast, px, py, pz, target, h, viewing_distance,
+                                       stg, stage_n);
     write_hit(s, out, i, h);
     if (kCount) write_counters(out, i, h);
   }
@@ -183,20 +189,23 @@ __global__ void __launch_bounds__(128) lod_grid_kernel(SceneView s, RaysView ray
 
 int g_cast_mode = 0;
 int g_host_transfer = 0;  // svo_set_host_transfer: 0 auto, 1 staged copies, 2 direct access
+int g_stage_depth = 0;    // svo_set_staging_depth: top levels the plain casts stage in shared memory
 
 // ------------------------------------------------------------------ device image
 uint64_t device_image_bytes(const svo_scene* sc) {
   const DeviceImage& d = sc->dev;
   if (!d.valid) return 0;
   const uint64_t len = sc->tree.arena.len(), W = len >= 32 ? len / 32 : 1;
-  return d.node_cap * sizeof(DevNode) + d.brick_cap * (len + W) * 4 + (d.color_cap + d.data_cap) * 4;
+  return d.node_cap * sizeof(DevNode) + d.brick_cap * (len + W) * 4 + (d.color_cap + d.data_cap) * 4 +
+         kMaxStaged * sizeof(DevNode);
 }
 uint64_t device_image_bytes_estimate(const svo_scene* sc) {
   const HostOctree& t = sc->tree;
   const uint64_t nn = t.nodes(), nb = std::max<uint64_t>(1, t.arena.slots());
   const uint64_t nc = std::max<uint64_t>(1, t.colors.size()), nd = std::max<uint64_t>(1, t.datas.size());
   const uint64_t len = t.arena.len(), W = len >= 32 ? len / 32 : 1;
-  return (nn + nn / 4 + 64) * sizeof(DevNode) + (nb + nb / 4 + 16) * (len + W) * 4 + (nc + nc / 4 + 64 + nd + nd / 4 + 64) * 4;
+  return (nn + nn / 4 + 64) * sizeof(DevNode) + (nb + nb / 4 + 16) * (len + W) * 4 + (nc + nc / 4 + 64 + nd + nd / 4 + 64) * 4 +
+         kMaxStaged * sizeof(DevNode);
 }
 
 SceneView scene_view(const svo_scene* sc) {
@@ -221,7 +230,13 @@ SceneView scene_view(const svo_scene* sc) {
   uint32_t levels = 0;
   for (uint32_t r = sc->tree.size / sc->tree.dim; r > 1; r >>= 1) ++levels;
   v.mip_top = (float)levels;
+  v.top = d.top;
   return v;
+}
+
+uint32_t staged_records(const svo_scene* sc, uint32_t depth) {
+  const DeviceImage& d = sc->dev;
+  return d.top ? d.top_count[std::min(depth, kMaxStageDepth)] : 0u;
 }
 
 namespace {
@@ -231,6 +246,7 @@ uint32_t vwords_of(const HostOctree& t) { return t.arena.len() >= 32 ? t.arena.l
 void build_node(const HostOctree& t, size_t k, DevNode& n) {
   std::memset(&n, 0, sizeof(n));
   for (auto& v : n.slot) v = kInvalidChild;
+  for (auto& v : n.stage) v = kNotStaged;  // set by stage_top for the nodes of the top table
   if (!t.reserved[k]) return;
   const uint32_t kind = t.kind[k];
   n.ocbits = t.stored_occupied_bits(k);
@@ -267,7 +283,68 @@ void build_vbits(const HostOctree& t, uint32_t slot, uint32_t* out) {
     if (!t.pix_empty(v[f])) out[f >> 5] |= 1u << (f & 31);
 }
 
+// The top table (breadth-first Internal nodes of depth < kMaxStageDepth) from the node records, and
+// every record's stage[] naming its staged children.  Records whose stage[] changes are marked dirty.
+void stage_top(HostOctree& t, DeviceImage& d) {
+  const uint64_t nn = d.host_nodes.size();
+  auto internal = [&](uint32_t k) {
+    return k < nn && (d.host_nodes[k].meta & 3u) == kInternal && (d.host_nodes[k].meta & 4u) != 0;
+  };
+  std::vector<uint32_t> keys;
+  std::vector<uint32_t> count(kMaxStageDepth + 1, 0);
+  if (internal(0)) keys.push_back(0);
+  count[1] = (uint32_t)keys.size();
+  size_t level = 0;
+  for (uint32_t depth = 1; depth < kMaxStageDepth; ++depth) {
+    const size_t end = keys.size();
+    for (size_t i = level; i < end; ++i)
+      for (int c = 0; c < 8; ++c) {
+        const uint32_t ck = d.host_nodes[keys[i]].slot[c];
+        if (ck != kInvalidChild && internal(ck) && std::find(keys.begin(), keys.end(), ck) == keys.end())
+          keys.push_back(ck);
+      }
+    level = end;
+    count[depth + 1] = (uint32_t)keys.size();
+  }
+  auto set_stage = [&](uint32_t k, const uint16_t (&st)[8]) {
+    if (std::memcmp(d.host_nodes[k].stage, st, sizeof(st)) != 0) {
+      std::memcpy(d.host_nodes[k].stage, st, sizeof(st));
+      if (k < t.node_dirty.size()) t.node_dirty[k] = 1;
+    }
+  };
+  const uint16_t none[8] = {kNotStaged, kNotStaged, kNotStaged, kNotStaged,
+                            kNotStaged, kNotStaged, kNotStaged, kNotStaged};
+  for (uint32_t k : d.top_keys)
+    if (k < nn && std::find(keys.begin(), keys.end(), k) == keys.end()) set_stage(k, none);
+  for (uint32_t k : keys) {
+    uint16_t st[8];
+    for (int c = 0; c < 8; ++c) {
+      const uint32_t ck = d.host_nodes[k].slot[c];
+      const auto at = ck == kInvalidChild ? keys.end() : std::find(keys.begin(), keys.end(), ck);
+      st[c] = at == keys.end() ? kNotStaged : (uint16_t)(at - keys.begin());
+    }
+    set_stage(k, st);
+  }
+  d.top_keys = keys;
+  for (uint32_t k = 0; k <= kMaxStageDepth; ++k) d.top_count[k] = count[k];
+}
+
+// Copies the top table's records from the node mirror to the device.
+svo_status upload_top(DeviceImage& d, cudaStream_t st) {
+  if (!d.top) SVO_CUDA_TRY(cudaMalloc(&d.top, kMaxStaged * sizeof(DevNode)));
+  d.host_top.resize(d.top_keys.size());
+  for (size_t i = 0; i < d.top_keys.size(); ++i) d.host_top[i] = d.host_nodes[d.top_keys[i]];
+  if (!d.host_top.empty())
+    SVO_CUDA_TRY(cudaMemcpyAsync(d.top, d.host_top.data(), d.host_top.size() * sizeof(DevNode),
+                                 cudaMemcpyHostToDevice, st));
+  return SVO_OK;
+}
+
 void free_device(DeviceImage& d) {
+  cudaFree(d.top);
+  d.top = nullptr;
+  d.top_keys.clear();
+  for (auto& c : d.top_count) c = 0;
   cudaFree(d.nodes);
   cudaFree(d.voxels);
   cudaFree(d.vbits);
@@ -298,6 +375,7 @@ svo_status full_upload(svo_scene* sc, cudaStream_t st) {
   try {
     d.host_nodes.assign(nn, DevNode{});
     for (uint64_t k = 0; k < nn; ++k) build_node(t, k, d.host_nodes[k]);
+    stage_top(t, d);
     d.host_vbits.assign(t.arena.slots() * (size_t)W, 0u);
     for (uint32_t sl = 0; sl < t.arena.slots(); ++sl) build_vbits(t, sl, &d.host_vbits[(size_t)sl * W]);
   } catch (const ReferencePanic& p) {
@@ -309,6 +387,10 @@ svo_status full_upload(svo_scene* sc, cudaStream_t st) {
   SVO_CUDA_TRY(cudaMalloc(&d.colors, d.color_cap * 4));
   SVO_CUDA_TRY(cudaMalloc(&d.datas, d.data_cap * 4));
   SVO_CUDA_TRY(cudaMemcpyAsync(d.nodes, d.host_nodes.data(), nn * sizeof(DevNode), cudaMemcpyHostToDevice, st));
+  {
+    const svo_status ts = upload_top(d, st);
+    if (ts != SVO_OK) return ts;
+  }
   if (t.arena.slots()) {
     SVO_CUDA_TRY(cudaMemcpyAsync(d.voxels, t.arena.raw().data(), (size_t)t.arena.slots() * len * 4,
                                  cudaMemcpyHostToDevice, st));
@@ -362,6 +444,7 @@ svo_status incremental_sync(svo_scene* sc, cudaStream_t st) {
     d.host_nodes.resize(nn);
     for (uint64_t k = 0; k < nn; ++k)
       if (t.node_dirty[k]) build_node(t, k, d.host_nodes[k]);
+    stage_top(t, d);  // rebuilt records lost their stage indices, and the top levels may have changed
     d.host_vbits.resize((size_t)t.arena.slots() * W, 0u);
     auto& bd = t.arena.dirty();
     for (uint32_t sl = 0; sl < t.arena.slots(); ++sl)
@@ -374,6 +457,8 @@ svo_status incremental_sync(svo_scene* sc, cudaStream_t st) {
                                  cudaMemcpyHostToDevice, st));
     return SVO_OK;
   });
+  if (rc != SVO_OK) return rc;
+  rc = upload_top(d, st);
   if (rc != SVO_OK) return rc;
   rc = copy_runs(t.arena.dirty(), t.arena.slots(), [&](uint64_t a, uint64_t b) -> svo_status {
     SVO_CUDA_TRY(cudaMemcpyAsync(d.voxels + a * len, t.arena.raw().data() + a * len, (b - a) * len * 4,
@@ -418,10 +503,20 @@ svo_status launch_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const sv
       const uint64_t grid = std::min<uint64_t>((uint64_t)q->sm_count * per_sm, (n + block - 1) / block);
       SVO_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st));
       const ClaimOrder order = claim_order(n, row, in_place ? 4 : 3);
-      if (count)
+      const uint32_t stage_n = g_cast_mode == 1 ? 0u : staged_records(sc, (uint32_t)g_stage_depth);
+      if (stage_n) {
+        // the staged records take dynamic shared memory: resident blocks from this launch's size
+        const size_t smem = (size_t)stage_n * sizeof(DevNode);
+        auto kern = count ? queue_kernel<true, false, true> : queue_kernel<false, false, true>;
+        int per = 0;
+        SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, block, smem));
+        const uint64_t sgrid = std::min<uint64_t>((uint64_t)q->sm_count * std::max(per, 1), (n + block - 1) / block);
+        kern<<<(unsigned)sgrid, block, smem, st>>>(v, rv, hv, n, order, ctr, 0.0f, stage_n);
+      } else if (count) {
         queue_kernel<true><<<(unsigned)grid, block, 0, st>>>(v, rv, hv, n, order, ctr);
-      else
+      } else {
         queue_kernel<false><<<(unsigned)grid, block, 0, st>>>(v, rv, hv, n, order, ctr);
+      }
       SVO_CUDA_TRY(cudaGetLastError());
       return SVO_OK;
     }
@@ -688,6 +783,13 @@ svo_status svo_cast_host(svo_scene* sc, const svo_rays* rays, uint64_t n, const 
 svo_status svo_set_host_transfer(int32_t mode) {
   if (mode < 0 || mode > 2) return fail(SVO_ERR_ARGUMENT, "svo_set_host_transfer: mode must be 0, 1 or 2");
   g_host_transfer = mode;
+  return SVO_OK;
+}
+
+svo_status svo_set_staging_depth(int32_t depth) {
+  if (depth < 0 || depth > (int32_t)kMaxStageDepth)
+    return fail(SVO_ERR_ARGUMENT, "svo_set_staging_depth: depth must be 0.." + std::to_string(kMaxStageDepth));
+  g_stage_depth = depth;
   return SVO_OK;
 }
 

@@ -18,12 +18,21 @@ struct alignas(64) DevNode {
   uint32_t meta;     // [1:0] content kind, [2] reserved, [23:8] 2-bit brick kind per octant,
                      // [25:24] MIP brick kind (3: the key has no node_mips entry)
   uint32_t mip;      // the node's MIP brick: Solid value or arena slot
-  uint32_t pad1[4];
+  uint16_t stage[8]; // Internal: the child's index in the scene's top table, kNotStaged when it has none
   uint32_t slot[8];  // Internal: child key or kInvalidChild; Leaf: brick per octant; UniformLeaf: slot[0]
 };
 static_assert(sizeof(DevNode) == 64, "DevNode must be 64 bytes");
 
 constexpr uint32_t kInvalidChild = 0xFFFFFFFFu;
+
+// Top table of a scene: its Internal nodes of depth < kMaxStageDepth (the root has depth 0) in
+// breadth-first order, children in octant order, so the nodes of depth < K are the table's first
+// top_count[K] records.  A cast with staging depth K copies those records into shared memory and
+// reads them from there; a node key with kStagedBit set is an index into that copy.
+constexpr uint32_t kMaxStageDepth = 4;
+constexpr uint32_t kMaxStaged = 1 + 8 + 64 + 512;  // records of depth < 4
+constexpr uint16_t kNotStaged = 0xFFFFu;
+constexpr uint32_t kStagedBit = 0x80000000u;
 
 // svo_hits is an array of kHitFields pointers; bytes per ray of each field, in declaration order.
 constexpr int kHitFields = 18;
@@ -49,6 +58,7 @@ struct SceneView {
   uint32_t literal; // 1: every ray takes the literal form of the cast (diagnostics)
   uint32_t mips;    // MIP maps enabled (get_by_ray_at_lod reads node MIPs)
   float mip_top;    // log2(size / D): the MIP level the LOD cast starts at (an integer)
+  const DevNode* top;  // the top table (breadth-first Internal nodes of depth < kMaxStageDepth)
 };
 
 // Cast form selected by svo_set_cast_mode (0 automatic, 1 literal only).
@@ -64,6 +74,10 @@ struct DeviceImage {
   uint32_t* datas = nullptr;
   uint64_t node_cap = 0, brick_cap = 0, color_cap = 0, data_cap = 0;
   uint64_t n_nodes = 0, n_bricks = 0, n_colors = 0, n_datas = 0;
+  DevNode* top = nullptr;                         // kMaxStaged records
+  uint32_t top_count[kMaxStageDepth + 1] = {};    // records of depth < K, K = 0..kMaxStageDepth
+  std::vector<uint32_t> top_keys;                 // node key of each top-table record
+  std::vector<DevNode> host_top;                  // the records as uploaded
   bool valid = false;
   // host mirror of the node records and voxel bits (source of in-place syncs)
   std::vector<DevNode> host_nodes;
@@ -95,4 +109,6 @@ uint64_t device_image_bytes_estimate(const svo_scene* s);
 void set_error(const std::string& msg);
 svo_status fail(svo_status code, const std::string& msg);
 SceneView scene_view(const svo_scene* s);
+// records of the top table that a cast with staging depth `depth` copies (0 when the scene has none)
+uint32_t staged_records(const svo_scene* s, uint32_t depth);
 }  // namespace svo

@@ -21,13 +21,15 @@ def items_of(*specs):
     return [(FakeScene(s, d), {}, n, {}, row) for s, d, n, row in specs]
 
 
-def fake_time(best):
+def fake_time(best, best_stage=0):
     seen = []
 
     def time_fn(cfg):
         key = (cfg.block, cfg.rays_per_chunk, cfg.blocks_per_sm, cfg.block_shape, cfg.sort_key)
-        seen.append(key)
-        return 1.0 if key == best else 2.0 + 0.001 * len(seen)
+        seen.append(key + (cfg.staging_depth,))
+        if key != best:
+            return 2.0 + 0.001 * len(seen)
+        return 1.0 - 0.1 * (cfg.staging_depth == best_stage)  # the best knobs, fastest at depth best_stage
 
     return time_fn, seen
 
@@ -45,9 +47,23 @@ def test_sweep_covers_the_knobs_of_the_batch(rows, want_shapes, want_sorts):
     assert {k[3] for k in seen} == want_shapes
     assert {k[4] for k in seen} == want_sorts
     assert {k[0] for k in seen} == set(autotune.BLOCKS) and {k[1] for k in seen} == set(autotune.CHUNKS)
-    assert len(seen) == len(set(seen)) == len(autotune.BLOCKS) * len(autotune.CHUNKS) * len(want_shapes) * len(want_sorts)
+    first = len(autotune.BLOCKS) * len(autotune.CHUNKS) * len(want_shapes) * len(want_sorts)
+    assert len(seen) == len(set(seen)) == first + len(autotune.STAGING)
+    assert all(k[5] == 0 for k in seen[:first])  # the first stage at staging depth 0
+    assert [k[:5] for k in seen[first:]] == [best] * len(autotune.STAGING)  # then the depths on the best
+    assert {k[5] for k in seen[first:]} == set(autotune.STAGING)
     assert (cfg.block, cfg.rays_per_chunk, cfg.blocks_per_sm, cfg.block_shape, cfg.sort_key) == best
-    assert info["cached"] is False and info["config"] == list(best)
+    assert cfg.staging_depth == 0
+    assert info["cached"] is False and info["config"] == list(best) + [0]
+
+
+@pytest.mark.parametrize("depth", [0, 2, 4])
+def test_staging_depth_is_kept_only_when_faster(depth):
+    items = items_of((512, 8, 100000, 0))
+    best = (64, 32, 0, 0, 1)
+    time_fn, seen = fake_time(best, best_stage=depth)
+    cfg, info = autotune.tune(None, items, "gpu", time_fn, use_cache=False)
+    assert cfg.staging_depth == depth and info["config"][5] == depth
 
 
 def test_empty_items_do_not_ask_for_the_sort():
@@ -68,18 +84,19 @@ def test_cache_round_trip_and_older_entries(tmp_path, monkeypatch):
     cfg2, info2 = autotune.tune(None, items, "GB300", time_fn)
     assert info2["cached"] and len(seen) == n  # no second sweep
     assert (cfg2.block, cfg2.rays_per_chunk, cfg2.blocks_per_sm, cfg2.block_shape, cfg2.sort_key) == best
+    assert cfg2.staging_depth == cfg.staging_depth
     # another GPU name or workload class is tuned on its own
     autotune.tune(None, items, "other", time_fn)
     assert len(seen) > n
-    # an entry with four knobs (no sort key) reads as index order
+    # an entry with four knobs (no sort key, no staging depth) reads as index order, nothing staged
     with open(autotune.CACHE) as f:
         cache = json.load(f)
-    key = "GB300|%s|sort" % autotune.signature(items)
+    key = "GB300|%s|stage" % autotune.signature(items)
     cache[key]["config"] = [64, 128, 0, 4]
     with open(autotune.CACHE, "w") as f:
         json.dump(cache, f)
     cfg3, _ = autotune.tune(None, items, "GB300", time_fn)
-    assert (cfg3.block, cfg3.rays_per_chunk, cfg3.block_shape, cfg3.sort_key) == (64, 128, 4, 0)
+    assert (cfg3.block, cfg3.rays_per_chunk, cfg3.block_shape, cfg3.sort_key, cfg3.staging_depth) == (64, 128, 4, 0, 0)
 
 
 def test_signature_buckets_the_workload():
@@ -99,3 +116,4 @@ def test_launch_count_of_a_batched_call():
     assert bench.batched_launches([rnd, rnd], 1) == 6
     assert bench.batched_launches([cam, empty], 1) == 1
     assert LaunchConfig(1, 2, 3, 4, 1).sort_key == 1 and LaunchConfig().sort_key == 0
+    assert LaunchConfig(1, 2, 3, 4, 1, 3).staging_depth == 3 and LaunchConfig().staging_depth == 0

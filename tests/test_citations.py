@@ -7,7 +7,6 @@ components (`insert.rs`, `update/mod.rs`): it then has to fit at least one refer
 """
 import os
 import re
-import subprocess
 
 import pytest
 
@@ -18,9 +17,13 @@ SOURCES = ["include/svo.h", "INTEGRATION.md"]
 
 
 def _cited_files():
-    tracked = subprocess.check_output(["git", "ls-files"], cwd=ROOT, text=True).split()
-    return SOURCES + [f for f in tracked if f.startswith(("shocovox_gb300/", "oracle/"))
-                      and f.endswith((".h", ".cuh", ".cu", ".cpp", ".py"))]
+    out = list(SOURCES)
+    for top in ("shocovox_gb300", "oracle"):
+        for d, dirs, names in os.walk(os.path.join(ROOT, top)):
+            dirs[:] = sorted(x for x in dirs if not x.startswith(("_", ".")))  # build output, caches
+            out += sorted(os.path.relpath(os.path.join(d, n), ROOT) for n in names
+                          if n.endswith((".h", ".cuh", ".cu", ".cpp", ".py")))
+    return out
 
 
 @pytest.fixture(scope="module")
