@@ -198,6 +198,16 @@ svo_status svo_scene_upload(svo_scene* scene, void* stream);
  * device allocation). */
 svo_status svo_scene_sync(svo_scene* scene, void* stream);
 svo_status svo_scene_release_device(svo_scene* scene);
+/* Device memory of scene images from the caller's allocator (process-wide) instead of cudaMalloc /
+ * cudaFree: for callers that pool device memory or cap it themselves.  `alloc` gets the byte count
+ * and the stream of the upload and returns device memory (at least 256-byte aligned) or NULL, which
+ * makes the upload return SVO_ERR_OUT_OF_MEMORY after releasing what it had taken (the scene is then
+ * left without a device image); `release` frees what `alloc` returned.  Both NULL restores
+ * cudaMalloc / cudaFree.  Change it only while no scene holds a device image from the other one.
+ * No counterpart in the reference (the Bevy plugin's buffers belong to wgpu). */
+typedef void* (*svo_alloc_fn)(size_t bytes, void* stream, void* user);
+typedef void (*svo_free_fn)(void* ptr, void* user);
+svo_status svo_set_device_allocator(svo_alloc_fn alloc, svo_free_fn release, void* user);
 
 /* ---- the hot path: Octree::get_by_ray (src/raytracing/raytracing_on_cpu.rs:316-565) ---- */
 /* n rays in device memory -> per-ray hits in device memory.  Allocates nothing.

@@ -120,6 +120,7 @@ SIGNATURES = {
     "svo_scene_upload": (_I32, [_VP, _VP]),
     "svo_scene_sync": (_I32, [_VP, _VP]),
     "svo_scene_release_device": (_I32, [_VP]),
+    "svo_set_device_allocator": (_I32, [_VP, _VP, _VP]),
     "svo_cast": (_I32, [_VP, _P(Rays), _U64, _P(Hits), _VP]),
     "svo_cast_host": (_I32, [_VP, _P(Rays), _U64, _P(Hits), _VP]),
     "svo_cast_lod": (_I32, [_VP, _P(Rays), _U64, _P(Hits), ctypes.c_float, _VP]),

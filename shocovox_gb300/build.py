@@ -18,7 +18,7 @@ LIB = os.path.join(OUT_DIR, "libsvo.so")
 
 HOST_SOURCES = ["svo_octree.cpp", "svo_capi.cpp", "svo_scenes.cpp", "svo_persist.cpp", "svo_vox.cpp"]
 CUDA_SOURCES = ["svo_device.cu", "svo_batch.cu", "svo_server.cu", "svo_render.cu"]
-HEADERS = ["svo_octree.h", "svo_internal.h", "svo_cast.cuh", "svo_restart.h", "svo_queue.h", "svo_lod.h"]
+HEADERS = ["svo_octree.h", "svo_internal.h", "svo_cast.cuh", "svo_restart.h", "svo_queue.h", "svo_lod.h", "svo_trace.h"]
 
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wextra",
             "-Wno-unused-parameter"]
@@ -51,10 +51,12 @@ def build(force=False, verbose=False, extra_nvcc=()):
     os.makedirs(OUT_DIR, exist_ok=True)
     nvcc = _nvcc()
     cxx = os.environ.get("CXX", "g++")
+    # the host sources include the toolkit's header-only NVTX (svo_trace.h)
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "include")
     objs, procs = [], []
     for src in HOST_SOURCES:
         obj = os.path.join(OUT_DIR, src.replace(".cpp", ".o"))
-        cmd = [cxx] + CXXFLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [cxx] + CXXFLAGS + ["-I", cuda_inc, "-c", os.path.join(CSRC, src), "-o", obj]
         procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
         objs.append(obj)
     for src in CUDA_SOURCES:
@@ -72,7 +74,7 @@ def build(force=False, verbose=False, extra_nvcc=()):
     if failed:
         raise RuntimeError("libsvo build failed: %s" % ", ".join(failed))
     tmp = LIB + ".tmp"
-    cmd = [nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", tmp] + objs + ["-lpthread"]
+    cmd = [nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", tmp] + objs + ["-lpthread", "-ldl"]
     subprocess.check_call(cmd)
     os.replace(tmp, LIB)
     return LIB

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "svo_cast.cuh"
+#include "svo_trace.h"
 
 namespace svo {
 
@@ -677,6 +678,7 @@ void svo_batch_workspace_destroy(svo_batch_workspace* ws) {
 
 svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items, uint32_t n_items,
                             const svo_launch_config* cfg, void* stream) {
+  TraceRange range("svo_cast_batched");
   if (!ws || (!items && n_items)) return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: NULL argument");
   if (n_items == 0) return SVO_OK;
   cudaStream_t st = (cudaStream_t)stream;
@@ -878,6 +880,7 @@ extern "C" {
 
 svo_status svo_cast_batched_noalloc(const svo_batch_item* items, uint32_t n_items, const svo_launch_config* cfg,
                                     void* stream) {
+  TraceRange range("svo_cast_batched_noalloc");
   if (!items && n_items) return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: NULL items");
   if (n_items > kNoAllocMaxItems)
     return fail(SVO_ERR_ARGUMENT, "svo_cast_batched_noalloc: " + std::to_string(n_items) + " items exceed the maximum of " +

@@ -8,6 +8,7 @@
 #include <string>
 
 #include "svo_internal.h"
+#include "svo_trace.h"
 
 namespace svo {
 namespace {
@@ -205,6 +206,7 @@ svo_status svo_clear_at_lod(svo_scene* s, uint32_t x, uint32_t y, uint32_t z, ui
 }
 
 svo_status svo_apply_ops(svo_scene* s, const svo_op* ops, uint64_t n, uint64_t* n_done) {
+  TraceRange range("svo_apply_ops");
   if (!s || (!ops && n)) return fail(SVO_ERR_ARGUMENT, "svo_apply_ops: NULL argument");
   uint64_t i = 0;
   svo_status rc = SVO_OK;

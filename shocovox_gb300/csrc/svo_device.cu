@@ -14,8 +14,48 @@
 
 #include "svo_cast.cuh"
 #include "svo_queue.h"
+#include "svo_trace.h"
 
 namespace svo {
+
+// Device memory of scene images: cudaMalloc / cudaFree, or the caller's allocator
+// (svo_set_device_allocator).
+struct ImageAllocator {
+  svo_alloc_fn alloc = nullptr;
+  svo_free_fn release = nullptr;
+  void* user = nullptr;
+};
+ImageAllocator g_image_alloc;
+std::mutex g_image_alloc_mutex;
+
+svo_status image_alloc(void** p, size_t bytes, cudaStream_t st) {
+  ImageAllocator a;
+  {
+    std::lock_guard<std::mutex> lock(g_image_alloc_mutex);
+    a = g_image_alloc;
+  }
+  *p = nullptr;
+  if (a.alloc) {
+    *p = a.alloc(bytes, (void*)st, a.user);
+    if (!*p) return fail(SVO_ERR_OUT_OF_MEMORY, "scene image: the device allocator returned no memory");
+    return SVO_OK;
+  }
+  SVO_CUDA_TRY(cudaMalloc(p, bytes));
+  return SVO_OK;
+}
+
+void image_free(void* p) {
+  if (!p) return;
+  ImageAllocator a;
+  {
+    std::lock_guard<std::mutex> lock(g_image_alloc_mutex);
+    a = g_image_alloc;
+  }
+  if (a.release)
+    a.release(p, a.user);
+  else
+    cudaFree(p);
+}
 
 template <bool kCount>
 __global__ void __launch_bounds__(128, 7) cast_kernel(SceneView s, RaysView rays, HitsView out, uint64_t n) {
@@ -331,7 +371,12 @@ void stage_top(HostOctree& t, DeviceImage& d) {
 
 // Copies the top table's records from the node mirror to the device.
 svo_status upload_top(DeviceImage& d, cudaStream_t st) {
-  if (!d.top) SVO_CUDA_TRY(cudaMalloc(&d.top, kMaxStaged * sizeof(DevNode)));
+  if (!d.top) {
+    void* p = nullptr;
+    const svo_status rc = image_alloc(&p, kMaxStaged * sizeof(DevNode), st);
+    if (rc != SVO_OK) return rc;
+    d.top = static_cast<DevNode*>(p);
+  }
   d.host_top.resize(d.top_keys.size());
   for (size_t i = 0; i < d.top_keys.size(); ++i) d.host_top[i] = d.host_nodes[d.top_keys[i]];
   if (!d.host_top.empty())
@@ -341,15 +386,15 @@ svo_status upload_top(DeviceImage& d, cudaStream_t st) {
 }
 
 void free_device(DeviceImage& d) {
-  cudaFree(d.top);
+  image_free(d.top);
   d.top = nullptr;
   d.top_keys.clear();
   for (auto& c : d.top_count) c = 0;
-  cudaFree(d.nodes);
-  cudaFree(d.voxels);
-  cudaFree(d.vbits);
-  cudaFree(d.colors);
-  cudaFree(d.datas);
+  image_free(d.nodes);
+  image_free(d.voxels);
+  image_free(d.vbits);
+  image_free(d.colors);
+  image_free(d.datas);
   d.nodes = nullptr;
   d.voxels = d.vbits = d.colors = d.datas = nullptr;
   d.node_cap = d.brick_cap = d.color_cap = d.data_cap = 0;
@@ -381,15 +426,32 @@ svo_status full_upload(svo_scene* sc, cudaStream_t st) {
   } catch (const ReferencePanic& p) {
     return fail(SVO_ERR_REFERENCE_PANIC, std::string("upload: ") + p.what());
   }
-  SVO_CUDA_TRY(cudaMalloc(&d.nodes, d.node_cap * sizeof(DevNode)));
-  SVO_CUDA_TRY(cudaMalloc(&d.voxels, d.brick_cap * (size_t)len * 4));
-  SVO_CUDA_TRY(cudaMalloc(&d.vbits, d.brick_cap * (size_t)W * 4));
-  SVO_CUDA_TRY(cudaMalloc(&d.colors, d.color_cap * 4));
-  SVO_CUDA_TRY(cudaMalloc(&d.datas, d.data_cap * 4));
+  {
+    // a failed allocation releases what the upload holds: the scene is left without a device image
+    void* p[5] = {};
+    const size_t bytes[5] = {d.node_cap * sizeof(DevNode), d.brick_cap * (size_t)len * 4, d.brick_cap * (size_t)W * 4,
+                             d.color_cap * 4, d.data_cap * 4};
+    for (int i = 0; i < 5; ++i) {
+      const svo_status rc = image_alloc(&p[i], bytes[i], st);
+      if (rc != SVO_OK) {
+        for (int j = 0; j < i; ++j) image_free(p[j]);
+        free_device(d);
+        return rc;
+      }
+    }
+    d.nodes = static_cast<DevNode*>(p[0]);
+    d.voxels = static_cast<uint32_t*>(p[1]);
+    d.vbits = static_cast<uint32_t*>(p[2]);
+    d.colors = static_cast<uint32_t*>(p[3]);
+    d.datas = static_cast<uint32_t*>(p[4]);
+  }
   SVO_CUDA_TRY(cudaMemcpyAsync(d.nodes, d.host_nodes.data(), nn * sizeof(DevNode), cudaMemcpyHostToDevice, st));
   {
     const svo_status ts = upload_top(d, st);
-    if (ts != SVO_OK) return ts;
+    if (ts != SVO_OK) {
+      free_device(d);
+      return ts;
+    }
   }
   if (t.arena.slots()) {
     SVO_CUDA_TRY(cudaMemcpyAsync(d.voxels, t.arena.raw().data(), (size_t)t.arena.slots() * len * 4,
@@ -657,18 +719,29 @@ using namespace svo;
 
 extern "C" {
 
+svo_status svo_set_device_allocator(svo_alloc_fn alloc, svo_free_fn release, void* user) {
+  if ((alloc == nullptr) != (release == nullptr))
+    return fail(SVO_ERR_ARGUMENT, "svo_set_device_allocator: give both functions or neither");
+  std::lock_guard<std::mutex> lock(g_image_alloc_mutex);
+  g_image_alloc = ImageAllocator{alloc, release, user};
+  return SVO_OK;
+}
+
 svo_status svo_scene_upload(svo_scene* sc, void* stream) {
+  TraceRange range("svo_scene_upload");
   if (!sc) return fail(SVO_ERR_ARGUMENT, "NULL scene");
   return full_upload(sc, (cudaStream_t)stream);
 }
 
 svo_status svo_scene_sync(svo_scene* sc, void* stream) {
+  TraceRange range("svo_scene_sync");
   if (!sc) return fail(SVO_ERR_ARGUMENT, "NULL scene");
   if (!sc->dev.valid) return full_upload(sc, (cudaStream_t)stream);
   return incremental_sync(sc, (cudaStream_t)stream);
 }
 
 svo_status svo_scene_release_device(svo_scene* sc) {
+  TraceRange range("svo_scene_release_device");
   if (!sc) return fail(SVO_ERR_ARGUMENT, "NULL scene");
   destroy_pipeline(sc->dev);
   free_device(sc->dev);
@@ -688,6 +761,7 @@ void svo_scene_destroy(svo_scene* sc) {
 
 svo_status svo_cast_rows(svo_scene* sc, const svo_rays* rays, uint64_t n, uint32_t row_length, const svo_hits* hits,
                          void* stream) {
+  TraceRange range("svo_cast");
   if (!sc || !rays || !hits) return fail(SVO_ERR_ARGUMENT, "svo_cast: NULL argument");
   if (!sc->dev.valid) return fail(SVO_ERR_NOT_UPLOADED, "svo_cast: scene has no device image (svo_scene_upload)");
   if (n && (!rays->ox || !rays->oy || !rays->oz || !rays->dx || !rays->dy || !rays->dz))
@@ -701,6 +775,7 @@ svo_status svo_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const svo_h
 
 svo_status svo_cast_lod_rows(svo_scene* sc, const svo_rays* rays, uint64_t n, uint32_t row, const svo_hits* hits,
                              float viewing_distance, void* stream) {
+  TraceRange range("svo_cast_lod");
   if (!sc || !rays || !hits) return fail(SVO_ERR_ARGUMENT, "NULL argument");
   if (!sc->dev.valid) return fail(SVO_ERR_NOT_UPLOADED, "svo_cast_lod: scene not uploaded");
   if (n == 0) return SVO_OK;
@@ -748,6 +823,7 @@ svo_status svo_cast_lod(svo_scene* sc, const svo_rays* rays, uint64_t n, const s
 
 svo_status svo_cast_host_rows(svo_scene* sc, const svo_rays* rays, uint64_t n, uint32_t row_length,
                               const svo_hits* hits, void* stream) {
+  TraceRange range("svo_cast_host");
   if (!sc || !rays || !hits) return fail(SVO_ERR_ARGUMENT, "svo_cast_host: NULL argument");
   if (!sc->dev.valid) return fail(SVO_ERR_NOT_UPLOADED, "svo_cast_host: scene has no device image");
   if (n == 0) return SVO_OK;

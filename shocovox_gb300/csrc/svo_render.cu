@@ -14,6 +14,7 @@
 
 #include "svo_cast.cuh"
 #include "svo_queue.h"
+#include "svo_trace.h"
 
 namespace svo {
 namespace {
@@ -278,6 +279,7 @@ svo_status render_views(svo_scene* sc, const svo_viewport* vps, uint32_t n_views
 
 extern "C" svo_status svo_render_viewports(svo_scene* sc, const svo_viewport* vps, uint32_t n_views, uint32_t W,
                                            uint32_t H, uint8_t* rgba, unsigned long long* unshaded, void* stream) {
+  TraceRange range("svo_render_viewports");
   if (!sc || (!vps && n_views)) return fail(SVO_ERR_ARGUMENT, "svo_render_viewports: NULL argument");
   if (W == 0 || H == 0 || n_views == 0) return SVO_OK;
   if (!rgba) return fail(SVO_ERR_ARGUMENT, "svo_render_viewports: NULL output");

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "svo_cast.cuh"
+#include "svo_trace.h"
 
 namespace svo {
 namespace {
@@ -137,6 +138,7 @@ uint64_t resident_bytes(const svo_server* sv, size_t n_scenes) {
 // Makes every scene of the batch resident, evicting idle least-recently-used ones above the budget.
 svo_status make_resident(svo_server* sv, const std::vector<uint32_t>& need, size_t n_scenes, cudaStream_t st,
                          LaunchCounts& cnt) {
+  TraceRange range("svo_server residency");
   for (uint32_t id : need) {
     SceneSlot& sc = sv->scenes[id];
     sc.last_used = ++sv->tick;
@@ -163,6 +165,7 @@ svo_status make_resident(svo_server* sv, const std::vector<uint32_t>& need, size
 }
 
 svo_status launch(svo_server* sv, LaunchSlot& ls, size_t n_scenes, LaunchCounts& cnt) {
+  TraceRange range("svo_server launch");
   uint64_t total = 0;
   size_t need = 0;
   for (Request* q : ls.reqs) {
@@ -234,6 +237,7 @@ void worker_main(svo_server* sv) {
     // retire finished launches
     for (LaunchSlot& ls : sv->slots) {
       if (!ls.busy || cudaEventQuery(ls.done) != cudaSuccess) continue;
+      TraceRange range("svo_server retire");
       const double t = now_s();
       for (Request* q : ls.reqs) {
         q->t_done = t;
