@@ -480,6 +480,22 @@ def run_single(args, w, workload):
             torch.cuda.synchronize()
             lib.svo_set_staging_depth(0)
             checks.append(("%s, staging depth 4" % ("svo_cast_rows" if row else "svo_cast"), host_fields(svo, outs)))
+
+        # the plain cast refilling idle lanes (svo_set_refill): park below T rays in flight
+        def refilled(t):
+            def run():
+                lib.svo_set_refill(t)
+                scene.cast(rp, hp, n, s, row_length=row)
+            return run
+        rf_reps = interleaved_repeats({t: refilled(t) for t in (0, 8, 16, 24)}, args.steps, 3, stream, torch)
+        lib.svo_set_refill(0)
+        refill_sweep = {"park_below%d" % t: spread(n * world, v) for t, v in rf_reps.items()}
+        if want_check:
+            lib.svo_set_refill(16)
+            scene.cast(rp, hp, n, s, row_length=row)
+            torch.cuda.synchronize()
+            lib.svo_set_refill(0)
+            checks.append(("%s, refill below 16" % ("svo_cast_rows" if row else "svo_cast"), host_fields(svo, outs)))
         ws = svo.BatchWorkspace()
         items = [(scene, rp, n, hp, row)]
         cfg, sweep = autotune_batched(svo, torch, ws, items, stream)
@@ -489,7 +505,8 @@ def run_single(args, w, workload):
                                                   "launches_per_step": batched_launches(items, cfg.sort_key)},
                                                  **cfg_record(cfg)),
                     "sweep_ms": sweep,
-                    "plain_staging_depth_sweep": stage_sweep}
+                    "plain_staging_depth_sweep": stage_sweep,
+                    "plain_refill_sweep": refill_sweep}
         if want_check:
             checks.append(("persistent batched kernel, autotuned", host_fields(svo, outs)))
     clk = clocks.stop()
@@ -609,20 +626,33 @@ def north_star_incoherent(args):
     rays = {k: torch.from_numpy(np.ascontiguousarray(a[:, i])).to(dev)
             for a, names in ((origins, RAY_KEYS[:3]), (dirs, RAY_KEYS[3:])) for i, k in enumerate(names)}
     rp = {k: v.data_ptr() for k, v in rays.items()}
-    outs = {v: device_outputs(torch, svo, n, dev, OUT_FIELDS) for v in ("plain", "index_order", "sorted")}
+    outs = {v: device_outputs(torch, svo, n, dev, OUT_FIELDS) for v in ("plain", "index_order", "sorted", "refill")}
     hp = {v: {k: t.data_ptr() for k, t in o.items()} for v, o in outs.items()}
     ws = svo.BatchWorkspace()
     items = {v: [(scene, rp, n, hp[v], 0)] for v in ("index_order", "sorted")}
     best, sweeps = {}, {}
     for v, key in (("index_order", 0), ("sorted", 1)):
         best[v], sweeps[v] = autotune_batched(svo, torch, ws, items[v], stream, fixed_sort=key)
+    lib = svo.lib()
+
+    def plain_cast(t, out):  # svo_cast, refilling idle lanes below t rays in flight (0: never)
+        def run():
+            lib.svo_set_refill(t)
+            scene.cast(rp, hp[out], n, s)
+        return run
+    # the refill threshold: a short sweep
+    t_sweep = interleaved_repeats({t: plain_cast(t, "refill") for t in (8, 16, 24)}, max(2, args.steps // 4), 1,
+                                  stream, torch)
+    t_best = min(t_sweep, key=lambda t: t_sweep[t][0])
     clocks = ClockSampler(0).start()
     for _ in range(args.warmup):
-        scene.cast(rp, hp["plain"], n, s)
-    reps = interleaved_repeats({"plain": lambda: scene.cast(rp, hp["plain"], n, s),
+        plain_cast(0, "plain")()
+    reps = interleaved_repeats({"plain": plain_cast(0, "plain"),
+                                "refill": plain_cast(t_best, "refill"),
                                 "index_order": lambda: ws.cast(items["index_order"], best["index_order"], s),
                                 "sorted": lambda: ws.cast(items["sorted"], best["sorted"], s)},
                                args.steps, REPEATS, stream, torch)
+    lib.svo_set_refill(0)
     clk = clocks.stop()
     got = {v: host_fields(svo, o) for v, o in outs.items()}
     oth.join()
@@ -631,7 +661,9 @@ def north_star_incoherent(args):
     cpu_s = time.perf_counter() - t0
     parity = merge_parity([compare_hits(got[v], ref, v) for v in got])
     plain = spread(n, reps["plain"])
-    res = {"svo_cast": plain}
+    res = {"svo_cast": plain,
+           "svo_cast_refill": dict(spread(n, reps["refill"]), park_below=t_best, vs_plain=versus(spread(n, reps["refill"]), plain),
+                                   sweep_ms={"park_below%d" % t: round(v[0], 4) for t, v in t_sweep.items()})}
     for v in ("index_order", "sorted"):
         c = best[v]
         res["batched_" + v] = dict(spread(n, reps[v]), launches_per_step=batched_launches(items[v], c.sort_key),

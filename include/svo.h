@@ -432,6 +432,12 @@ svo_status svo_set_host_transfer(int32_t mode);
  * The results are the same at every depth; the batched cast takes its depth from
  * svo_launch_config.staging_depth.  No counterpart in the reference. */
 svo_status svo_set_staging_depth(int32_t depth);
+/* Lane refill of the plain casts launched afterwards (process-wide): 0 (default) casts each warp's
+ * 32 rays to their ends; 1..32: a warp whose rays in flight drop below park_below stops them at their
+ * next node visit, gives its idle lanes new rays and continues all of them together, so that rays of
+ * very different lengths (rays in no particular order) keep the lanes busy.  The results are the same
+ * for every value.  No counterpart in the reference. */
+svo_status svo_set_refill(int32_t park_below);
 
 #ifdef __cplusplus
 }

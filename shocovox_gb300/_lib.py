@@ -147,6 +147,7 @@ SIGNATURES = {
     "svo_set_cast_mode": (_I32, [_I32]),
     "svo_set_host_transfer": (_I32, [_I32]),
     "svo_set_staging_depth": (_I32, [_I32]),
+    "svo_set_refill": (_I32, [_I32]),
 }
 
 

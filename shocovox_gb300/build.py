@@ -18,7 +18,8 @@ LIB = os.path.join(OUT_DIR, "libsvo.so")
 
 HOST_SOURCES = ["svo_octree.cpp", "svo_capi.cpp", "svo_scenes.cpp", "svo_persist.cpp", "svo_vox.cpp"]
 CUDA_SOURCES = ["svo_device.cu", "svo_batch.cu", "svo_server.cu", "svo_render.cu"]
-HEADERS = ["svo_octree.h", "svo_internal.h", "svo_cast.cuh", "svo_restart.h", "svo_queue.h", "svo_lod.h", "svo_trace.h"]
+HEADERS = ["svo_octree.h", "svo_internal.h", "svo_cast.cuh", "svo_restart.h", "svo_queue.h", "svo_lod.h", "svo_trace.h",
+           "svo_refill.cuh"]
 
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wextra",
             "-Wno-unused-parameter"]

@@ -14,6 +14,7 @@
 
 #include "svo_cast.cuh"
 #include "svo_queue.h"
+#include "svo_refill.cuh"
 #include "svo_trace.h"
 
 namespace svo {
@@ -182,6 +183,118 @@ __global__ void __launch_bounds__(128, 7)
   }
 }
 
+// Refilling cast: the work queue of queue_kernel, where a warp also parks its rays at a node visit
+// once fewer than park_below of them are in flight, hands its idle lanes new entering rays from its
+// waiting list (refilled from the work counter) and resumes all of them together.  Rays in no
+// particular order then keep the lanes busy where a warp would otherwise run its few longest rays
+// alone; park_below = 0 never parks (each warp's rays run to their end, as in queue_kernel).
+template <bool kCount, bool kStage = false>
+__global__ void __launch_bounds__(128, 7)
+    refill_kernel(SceneView s, RaysView rays, HitsView out, uint64_t n, ClaimOrder order,
+                  unsigned long long* __restrict__ counter, uint32_t park_below, uint32_t stage_n = 0) {
+  __shared__ SharedLuts L;
+  __shared__ WaitingRays waiting[4];
+  __shared__ uint32_t in_flight[4];  // rays of each warp in flight (parked ones included)
+  extern __shared__ uint4 staged_smem[];
+  DevNode* stg = reinterpret_cast<DevNode*>(staged_smem);
+  fill_shared_luts(L);
+  if (kStage) stage_records(stg, s.top, stage_n);
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31u;
+  WaitingRays& w = waiting[threadIdx.x >> 5];
+  volatile uint32_t* live = in_flight + (threadIdx.x >> 5);
+  uint32_t count = 0;  // rays waiting (the same in every lane)
+  bool more = true;    // claims left
+  uint32_t park = park_below;
+  bool alive = false;
+  uint64_t i = 0;
+  FastState st;
+  for (;;) {
+    const unsigned idle = __ballot_sync(0xFFFFFFFFu, !alive);
+    const uint32_t need = __popc(idle);
+    if (need) {
+      // claims until `need` entering rays wait or no claims are left (misses written at once)
+      while (more && count < need) {
+        unsigned long long c = 0;
+        if (lane == 0) c = atomicAdd(counter, 1ull);
+        c = __shfl_sync(0xFFFFFFFFu, c, 0);
+        if (c >= order.claims) {
+          more = false;
+          break;
+        }
+        const uint64_t j = claimed_ray(order, c, lane, n);
+        bool enters = false, fast = false;
+        float px = 0.0f, py = 0.0f, pz = 0.0f;
+        uint32_t target = 0;
+        if (j < n) {
+          const float ox = __ldg(rays.ox + j), oy = __ldg(rays.oy + j), oz = __ldg(rays.oz + j);
+          const float dx = __ldg(rays.dx + j), dy = __ldg(rays.dy + j), dz = __ldg(rays.dz + j);
+          fast = !s.literal && !isnan(dx) && !isnan(dy) && !isnan(dz);
+          enters = !fast || fast_entry(s, ox, oy, oz, dx, dy, dz, px, py, pz, target);
+          if (!enters) {
+            HitRecord m;
+            miss_record(m);
+            write_hit(s, out, j, m);
+            if (kCount) write_counters(out, j, m);
+          }
+        }
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, enters);
+        if (enters) {
+          const uint32_t k = count + __popc(m & ((1u << lane) - 1u));
+          w.p[0][k] = px;
+          w.p[1][k] = py;
+          w.p[2][k] = pz;
+          w.target[k] = target | (fast ? 0x80000000u : 0u);
+          w.i[k] = j;
+        }
+        count += __popc(m);
+        __syncwarp();
+      }
+      // the k-th idle lane takes the k-th of the last `take` waiting rays
+      const uint32_t take = count < need ? count : need;
+      if (!alive) {
+        const uint32_t k = __popc(idle & ((1u << lane) - 1u));
+        if (k < take) {
+          const uint32_t at = count - take + k;
+          i = w.i[at];
+          const uint32_t tg = w.target[at];
+          const float px = w.p[0][at], py = w.p[1][at], pz = w.p[2][at];
+          const float ox = __ldg(rays.ox + i), oy = __ldg(rays.oy + i), oz = __ldg(rays.oz + i);
+          const float dx = __ldg(rays.dx + i), dy = __ldg(rays.dy + i), dz = __ldg(rays.dz + i);
+          if ((tg >> 31) == 0u) {  // a NaN direction (or literal mode): the literal form, in one go
+            HitRecord h;
+            cast_ray_literal<kCount>(s, L, ox, oy, oz, dx, dy, dz, h);
+            write_hit(s, out, i, h);
+            if (kCount) write_counters(out, i, h);
+          } else {
+            fast_start(st, dx, dy, dz, px, py, pz, tg & 0x7FFFFFFFu);
+            alive = true;
+          }
+        }
+      }
+      count -= take;
+      if (take == 0 && !more) park = 0;  // nothing left to hand out: rays in flight run to their end
+      __syncwarp();
+      const unsigned now = __ballot_sync(0xFFFFFFFFu, alive);
+      if (lane == 0) *live = __popc(now);
+      __syncwarp();
+      if (now == 0) {
+        if (!more && count == 0) break;
+        continue;
+      }
+    }
+    if (alive) {
+      HitRecord h;
+      if (fast_run<kCount, kStage>(st, s, L, h, live, park, stg, stage_n)) {
+        write_hit(s, out, i, h);
+        if (kCount) write_counters(out, i, h);
+        alive = false;
+      }
+    }
+    __syncwarp();
+  }
+}
+
 constexpr uint64_t kQueueMinRays = 1u << 15;  // below this the one-thread-per-ray grid is as fast
 
 void destroy_queues(DeviceImage& d) {
@@ -230,6 +343,7 @@ __global__ void __launch_bounds__(128) lod_grid_kernel(SceneView s, RaysView ray
 int g_cast_mode = 0;
 int g_host_transfer = 0;  // svo_set_host_transfer: 0 auto, 1 staged copies, 2 direct access
 int g_stage_depth = 0;    // svo_set_staging_depth: top levels the plain casts stage in shared memory
+int g_refill_below = 0;   // svo_set_refill: a warp parks and refills below this many rays in flight
 
 // ------------------------------------------------------------------ device image
 uint64_t device_image_bytes(const svo_scene* sc) {
@@ -566,7 +680,15 @@ svo_status launch_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const sv
       SVO_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st));
       const ClaimOrder order = claim_order(n, row, in_place ? 4 : 3);
       const uint32_t stage_n = g_cast_mode == 1 ? 0u : staged_records(sc, (uint32_t)g_stage_depth);
-      if (stage_n) {
+      if (g_refill_below > 0) {
+        const size_t smem = (size_t)stage_n * sizeof(DevNode);
+        auto kern = stage_n ? (count ? refill_kernel<true, true> : refill_kernel<false, true>)
+                            : (count ? refill_kernel<true> : refill_kernel<false>);
+        int per = 0;
+        SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, block, smem));
+        const uint64_t rgrid = std::min<uint64_t>((uint64_t)q->sm_count * std::max(per, 1), (n + block - 1) / block);
+        kern<<<(unsigned)rgrid, block, smem, st>>>(v, rv, hv, n, order, ctr, (uint32_t)g_refill_below, stage_n);
+      } else if (stage_n) {
         // the staged records take dynamic shared memory: resident blocks from this launch's size
         const size_t smem = (size_t)stage_n * sizeof(DevNode);
         auto kern = count ? queue_kernel<true, false, true> : queue_kernel<false, false, true>;
@@ -859,6 +981,12 @@ svo_status svo_cast_host(svo_scene* sc, const svo_rays* rays, uint64_t n, const 
 svo_status svo_set_host_transfer(int32_t mode) {
   if (mode < 0 || mode > 2) return fail(SVO_ERR_ARGUMENT, "svo_set_host_transfer: mode must be 0, 1 or 2");
   g_host_transfer = mode;
+  return SVO_OK;
+}
+
+svo_status svo_set_refill(int32_t park_below) {
+  if (park_below < 0 || park_below > 32) return fail(SVO_ERR_ARGUMENT, "svo_set_refill: park_below must be 0..32");
+  g_refill_below = park_below;
   return SVO_OK;
 }
 
