@@ -29,7 +29,13 @@ struct ImageAllocator {
 ImageAllocator g_image_alloc;
 std::mutex g_image_alloc_mutex;
 
-svo_status image_alloc(void** p, size_t bytes, cudaStream_t st) {
+bool caller_allocator() {
+  std::lock_guard<std::mutex> lock(g_image_alloc_mutex);
+  return g_image_alloc.alloc != nullptr;
+}
+
+// `ordered`: from the stream-ordered pool on st (used only without the caller's allocator)
+svo_status image_alloc(void** p, size_t bytes, cudaStream_t st, bool ordered = false) {
   ImageAllocator a;
   {
     std::lock_guard<std::mutex> lock(g_image_alloc_mutex);
@@ -41,7 +47,11 @@ svo_status image_alloc(void** p, size_t bytes, cudaStream_t st) {
     if (!*p) return fail(SVO_ERR_OUT_OF_MEMORY, "scene image: the device allocator returned no memory");
     return SVO_OK;
   }
-  SVO_CUDA_TRY(cudaMalloc(p, bytes));
+  if (ordered) {
+    SVO_CUDA_TRY(cudaMallocAsync(p, bytes, st));
+  } else {
+    SVO_CUDA_TRY(cudaMalloc(p, bytes));
+  }
   return SVO_OK;
 }
 
@@ -487,7 +497,7 @@ void stage_top(HostOctree& t, DeviceImage& d) {
 svo_status upload_top(DeviceImage& d, cudaStream_t st) {
   if (!d.top) {
     void* p = nullptr;
-    const svo_status rc = image_alloc(&p, kMaxStaged * sizeof(DevNode), st);
+    const svo_status rc = image_alloc(&p, kMaxStaged * sizeof(DevNode), st, d.ordered);
     if (rc != SVO_OK) return rc;
     d.top = static_cast<DevNode*>(p);
   }
@@ -500,25 +510,39 @@ svo_status upload_top(DeviceImage& d, cudaStream_t st) {
 }
 
 void free_device(DeviceImage& d) {
-  image_free(d.top);
+  // cudaFree waits for no cast on memory from the stream-ordered pool: wait for the device here, as
+  // cudaFree does for other memory, so that releasing a scene keeps the same meaning either way
+  if (d.ordered && (d.top || d.nodes)) cudaDeviceSynchronize();
+  if (d.ordered) {
+    cudaFree(d.top);
+    cudaFree(d.nodes);
+    cudaFree(d.voxels);
+    cudaFree(d.vbits);
+    cudaFree(d.colors);
+    cudaFree(d.datas);
+  } else {
+    image_free(d.top);
+    image_free(d.nodes);
+    image_free(d.voxels);
+    image_free(d.vbits);
+    image_free(d.colors);
+    image_free(d.datas);
+  }
+  d.ordered = false;
   d.top = nullptr;
   d.top_keys.clear();
   for (auto& c : d.top_count) c = 0;
-  image_free(d.nodes);
-  image_free(d.voxels);
-  image_free(d.vbits);
-  image_free(d.colors);
-  image_free(d.datas);
   d.nodes = nullptr;
   d.voxels = d.vbits = d.colors = d.datas = nullptr;
   d.node_cap = d.brick_cap = d.color_cap = d.data_cap = 0;
   d.valid = false;
 }
 
-svo_status full_upload(svo_scene* sc, cudaStream_t st) {
+svo_status full_upload(svo_scene* sc, cudaStream_t st, bool ordered = false) {
   HostOctree& t = sc->tree;
   DeviceImage& d = sc->dev;
   free_device(d);
+  d.ordered = ordered && !caller_allocator();
   {
     const svo_status qs = create_queues(d);
     if (qs != SVO_OK) return qs;
@@ -546,9 +570,15 @@ svo_status full_upload(svo_scene* sc, cudaStream_t st) {
     const size_t bytes[5] = {d.node_cap * sizeof(DevNode), d.brick_cap * (size_t)len * 4, d.brick_cap * (size_t)W * 4,
                              d.color_cap * 4, d.data_cap * 4};
     for (int i = 0; i < 5; ++i) {
-      const svo_status rc = image_alloc(&p[i], bytes[i], st);
+      const svo_status rc = image_alloc(&p[i], bytes[i], st, d.ordered);
       if (rc != SVO_OK) {
-        for (int j = 0; j < i; ++j) image_free(p[j]);
+        for (int j = 0; j < i; ++j) {
+          if (d.ordered)
+            cudaFreeAsync(p[j], st);
+          else
+            image_free(p[j]);
+        }
+        d.ordered = false;
         free_device(d);
         return rc;
       }
@@ -838,6 +868,36 @@ __global__ void lut_kernel(uint64_t* rtn, uint32_t* step, uint64_t* mask) {
 }  // namespace svo
 
 using namespace svo;
+
+extern "C" {
+
+}  // extern "C"
+
+namespace svo {
+svo_status upload_ordered(svo_scene* sc, cudaStream_t st) {
+  TraceRange range("svo_scene_upload (stream-ordered)");
+  return full_upload(sc, st, true);
+}
+
+svo_status evict_ordered(svo_scene* sc, cudaStream_t st) {
+  TraceRange range("svo_scene_evict");
+  DeviceImage& d = sc->dev;
+  if (!d.ordered) return svo_scene_release_device(sc);
+  void* arrays[6] = {d.top, d.nodes, d.voxels, d.vbits, d.colors, d.datas};
+  for (void* p : arrays)
+    if (p) SVO_CUDA_TRY(cudaFreeAsync(p, st));
+  d.top = d.nodes = nullptr;
+  d.voxels = d.vbits = d.colors = d.datas = nullptr;
+  d.top_keys.clear();
+  for (auto& c : d.top_count) c = 0;
+  d.node_cap = d.brick_cap = d.color_cap = d.data_cap = 0;
+  d.valid = false;
+  d.ordered = false;
+  std::fill(sc->tree.node_dirty.begin(), sc->tree.node_dirty.end(), 1);
+  std::fill(sc->tree.arena.dirty().begin(), sc->tree.arena.dirty().end(), 1);
+  return SVO_OK;
+}
+}  // namespace svo
 
 extern "C" {
 

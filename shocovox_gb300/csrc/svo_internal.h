@@ -2,6 +2,8 @@
 // scene handle, the device image layout and the error reporting helpers.
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -79,6 +81,7 @@ struct DeviceImage {
   std::vector<uint32_t> top_keys;                 // node key of each top-table record
   std::vector<DevNode> host_top;                  // the records as uploaded
   bool valid = false;
+  bool ordered = false;  // image arrays from the stream-ordered pool (a server's residency)
   // host mirror of the node records and voxel bits (source of in-place syncs)
   std::vector<DevNode> host_nodes;
   std::vector<uint32_t> host_vbits;
@@ -109,6 +112,11 @@ uint64_t device_image_bytes_estimate(const svo_scene* s);
 void set_error(const std::string& msg);
 svo_status fail(svo_status code, const std::string& msg);
 SceneView scene_view(const svo_scene* s);
+// A server's residency: the image allocated from the stream-ordered pool on `st` (unless the caller's
+// allocator is installed), and given back the same way, so that evicting one scene and uploading
+// another does not wait for the whole device.  The evicted scene must have no cast in flight.
+svo_status upload_ordered(svo_scene* s, cudaStream_t st);
+svo_status evict_ordered(svo_scene* s, cudaStream_t st);
 // records of the top table that a cast with staging depth `depth` copies (0 when the scene has none)
 uint32_t staged_records(const svo_scene* s, uint32_t depth);
 }  // namespace svo

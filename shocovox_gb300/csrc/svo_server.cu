@@ -153,11 +153,12 @@ svo_status make_resident(svo_server* sv, const std::vector<uint32_t>& need, size
         if (victim < 0 || c.last_used < sv->scenes[victim].last_used) victim = (int)j;
       }
       if (victim < 0) break;  // nothing idle left to evict: admit over budget rather than deadlock
-      svo_status rc = svo_scene_release_device(sv->scenes[victim].scene);
+      // the victim's last launch has retired: its image goes back to the pool in stream order
+      svo_status rc = evict_ordered(sv->scenes[victim].scene, st);
       if (rc != SVO_OK) return rc;
       cnt.evictions++;
     }
-    svo_status rc = svo_scene_upload(sc.scene, st);
+    svo_status rc = upload_ordered(sc.scene, st);
     if (rc != SVO_OK) return rc;
     cnt.uploads++;
   }
