@@ -411,6 +411,9 @@ def run_single(args, w, workload):
 
     # camera rays in raster order: svo_cast_rows hands warps 8 x 4 blocks of neighbouring pixels
     row = ray_rows(w)
+    lib = svo.lib()
+    svo.check(lib.svo_set_refill(args.refill))  # the timed cast's knobs (0, 0: queue_kernel, nothing staged)
+    svo.check(lib.svo_set_staging_depth(args.staging_depth))
     clocks = ClockSampler(local_rank).start()  # samples from the warm-up on, so short timed regions get samples
     for _ in range(args.warmup):
         scene.cast(rp, hp, n, s, row_length=row)
@@ -464,7 +467,6 @@ def run_single(args, w, workload):
     variants = None
     if not args.no_variants:
         # the plain cast with the top tree levels staged in shared memory (svo_set_staging_depth)
-        lib = svo.lib()
 
         def staged(k):
             def run():
@@ -511,7 +513,9 @@ def run_single(args, w, workload):
             checks.append(("persistent batched kernel, autotuned", host_fields(svo, outs)))
     clk = clocks.stop()
 
-    # end to end through the host-buffer C-ABI call (pinned host memory)
+    # end to end through the host-buffer C-ABI call (pinned host memory), with the timed cast's knobs
+    lib.svo_set_refill(args.refill)
+    lib.svo_set_staging_depth(args.staging_depth)
     pin_cols = [torch.from_numpy(c).pin_memory() for c in cols_host]
     pin_out = {k: torch.empty(n, dtype=outs[k].dtype).pin_memory() for k in OUT_FIELDS}
     cols_np = [c.numpy() for c in pin_cols]
@@ -541,6 +545,8 @@ def run_single(args, w, workload):
         if want_check:
             checks.append(("host buffers, %s" % name, {k: v.copy() for k, v in out_np.items()}))
     svo.lib().svo_set_host_transfer(0)
+    lib.svo_set_refill(0)
+    lib.svo_set_staging_depth(0)
 
     # the oracle casts the whole batch once (all host threads): the CPU baseline and the parity reference
     cpu, parity = None, None
@@ -584,6 +590,7 @@ def run_single(args, w, workload):
                    "build_s": round(build_s, 1), "parallelism": "replicas" if world > 1 else "single",
                    "ray_order": ("rows of %d rays (svo_cast_rows: 8 x 4 ray blocks per warp)" % row) if row
                    else "as generated (svo_cast)",
+                   "timed_cast_knobs": {"refill_park_below": args.refill, "staging_depth": args.staging_depth},
                    "svo_cast_plain_order": plain},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_src,
@@ -1554,6 +1561,10 @@ def main():
     ap.add_argument("--no-north-star", action="store_true",
                     help="skip the incoherent1024 / multiscene64 / served16 comparisons of the default run")
     ap.add_argument("--no-variants", action="store_true", help="skip the persistent-kernel autotune sweep")
+    ap.add_argument("--refill", type=int, default=0,
+                    help="svo_set_refill for the timed plain cast: park a warp's rays below this many in flight")
+    ap.add_argument("--staging-depth", type=int, default=0,
+                    help="svo_set_staging_depth for the timed plain cast: top levels staged in shared memory")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.impl == "reference":

@@ -603,6 +603,7 @@ svo_status launch_claimed(const BatchItemDev* d_items, uint32_t n_items, uint64_
   const size_t smem = (size_t)staged_n * sizeof(DevNode);
   auto kern = staged_n ? (count ? batched_kernel<true, true> : batched_kernel<false, true>)
                        : (count ? batched_kernel<true> : batched_kernel<false>);
+  SVO_CUDA_TRY(allow_dynamic_smem(kern, smem));
   int per_sm = (cfg && cfg->blocks_per_sm) ? (int)cfg->blocks_per_sm : 0;
   if (per_sm == 0) {
     SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem));
@@ -815,6 +816,7 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
                                 : (count ? sorted_cast_kernel<true, false, true> : sorted_cast_kernel<false, false, true>))
                       : (single ? (count ? sorted_cast_kernel<true, true> : sorted_cast_kernel<false, true>)
                                 : (count ? sorted_cast_kernel<true, false> : sorted_cast_kernel<false, false>));
+    SVO_CUDA_TRY(allow_dynamic_smem(cast, smem));
     int per_sm = (cfg && cfg->blocks_per_sm) ? (int)cfg->blocks_per_sm : 0;
     if (per_sm == 0) {
       SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cast, block, smem));

@@ -1055,6 +1055,19 @@ struct RaysView {
   const float *ox, *oy, *oz, *dx, *dy, *dz;
 };
 
+// Lets `kernel` take `bytes` of dynamic shared memory: with its static shared memory a block may pass
+// 48 KB only after the opt-in, which is raised when a launch asks for more than allowed so far (never
+// lowered).  Host-side attributes only: nothing is enqueued.
+template <class K>
+inline cudaError_t allow_dynamic_smem(K kernel, size_t bytes) {
+  if (bytes == 0) return cudaSuccess;
+  cudaFuncAttributes a{};
+  cudaError_t e = cudaFuncGetAttributes(&a, (const void*)kernel);
+  if (e != cudaSuccess) return e;
+  if ((size_t)a.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+  return cudaFuncSetAttribute((const void*)kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 // Copies `n` top-table records from `src` (global) to `dst` (shared memory) with the block's threads,
 // 16 bytes per load.  The caller synchronises the block before the copy is read.
 __device__ __forceinline__ void stage_records(DevNode* dst, const DevNode* src, uint32_t n) {

@@ -714,6 +714,7 @@ svo_status launch_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const sv
         const size_t smem = (size_t)stage_n * sizeof(DevNode);
         auto kern = stage_n ? (count ? refill_kernel<true, true> : refill_kernel<false, true>)
                             : (count ? refill_kernel<true> : refill_kernel<false>);
+        SVO_CUDA_TRY(allow_dynamic_smem(kern, smem));
         int per = 0;
         SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, block, smem));
         const uint64_t rgrid = std::min<uint64_t>((uint64_t)q->sm_count * std::max(per, 1), (n + block - 1) / block);
@@ -722,6 +723,7 @@ svo_status launch_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const sv
         // the staged records take dynamic shared memory: resident blocks from this launch's size
         const size_t smem = (size_t)stage_n * sizeof(DevNode);
         auto kern = count ? queue_kernel<true, false, true> : queue_kernel<false, false, true>;
+        SVO_CUDA_TRY(allow_dynamic_smem(kern, smem));
         int per = 0;
         SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, block, smem));
         const uint64_t sgrid = std::min<uint64_t>((uint64_t)q->sm_count * std::max(per, 1), (n + block - 1) / block);
