@@ -489,7 +489,7 @@ def run_single(args, w, workload):
                 lib.svo_set_refill(t)
                 scene.cast(rp, hp, n, s, row_length=row)
             return run
-        rf_reps = interleaved_repeats({t: refilled(t) for t in (0, 8, 16, 24)}, args.steps, 3, stream, torch)
+        rf_reps = interleaved_repeats({t: refilled(t) for t in (0, 8, 16, 24, 32)}, args.steps, 3, stream, torch)
         lib.svo_set_refill(0)
         refill_sweep = {"park_below%d" % t: spread(n * world, v) for t, v in rf_reps.items()}
         if want_check:
@@ -648,7 +648,7 @@ def north_star_incoherent(args):
             scene.cast(rp, hp[out], n, s)
         return run
     # the refill threshold: a short sweep
-    t_sweep = interleaved_repeats({t: plain_cast(t, "refill") for t in (8, 16, 24)}, max(2, args.steps // 4), 1,
+    t_sweep = interleaved_repeats({t: plain_cast(t, "refill") for t in (8, 16, 24, 32)}, max(2, args.steps // 4), 1,
                                   stream, torch)
     t_best = min(t_sweep, key=lambda t: t_sweep[t][0])
     clocks = ClockSampler(0).start()
@@ -1058,6 +1058,8 @@ def run_served(args, w):
         svo.HIT_FIELDS[f]) for f in full_fields} for k in full_ids}
 
     def serve(srv, paced):
+        for t in scenes:  # every run starts with no scene resident
+            t.release_device()
         ids = [srv.add_scene(t) for t in scenes]
         assert ids == list(range(len(scenes)))
         # warm-up: the launch path exercised once per scene (scenes past the budget are evicted again)

@@ -11,6 +11,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 
 #include "svo_cast.cuh"
 #include "svo_queue.h"
@@ -455,8 +456,12 @@ void stage_top(HostOctree& t, DeviceImage& d) {
     return k < nn && (d.host_nodes[k].meta & 3u) == kInternal && (d.host_nodes[k].meta & 4u) != 0;
   };
   std::vector<uint32_t> keys;
+  std::unordered_map<uint32_t, uint32_t> index;  // node key -> its place in the table
   std::vector<uint32_t> count(kMaxStageDepth + 1, 0);
-  if (internal(0)) keys.push_back(0);
+  if (internal(0)) {
+    keys.push_back(0);
+    index[0] = 0;
+  }
   count[1] = (uint32_t)keys.size();
   size_t level = 0;
   for (uint32_t depth = 1; depth < kMaxStageDepth; ++depth) {
@@ -464,8 +469,7 @@ void stage_top(HostOctree& t, DeviceImage& d) {
     for (size_t i = level; i < end; ++i)
       for (int c = 0; c < 8; ++c) {
         const uint32_t ck = d.host_nodes[keys[i]].slot[c];
-        if (ck != kInvalidChild && internal(ck) && std::find(keys.begin(), keys.end(), ck) == keys.end())
-          keys.push_back(ck);
+        if (ck != kInvalidChild && internal(ck) && index.emplace(ck, (uint32_t)keys.size()).second) keys.push_back(ck);
       }
     level = end;
     count[depth + 1] = (uint32_t)keys.size();
@@ -479,13 +483,12 @@ void stage_top(HostOctree& t, DeviceImage& d) {
   const uint16_t none[8] = {kNotStaged, kNotStaged, kNotStaged, kNotStaged,
                             kNotStaged, kNotStaged, kNotStaged, kNotStaged};
   for (uint32_t k : d.top_keys)
-    if (k < nn && std::find(keys.begin(), keys.end(), k) == keys.end()) set_stage(k, none);
+    if (k < nn && !index.count(k)) set_stage(k, none);
   for (uint32_t k : keys) {
     uint16_t st[8];
     for (int c = 0; c < 8; ++c) {
-      const uint32_t ck = d.host_nodes[k].slot[c];
-      const auto at = ck == kInvalidChild ? keys.end() : std::find(keys.begin(), keys.end(), ck);
-      st[c] = at == keys.end() ? kNotStaged : (uint16_t)(at - keys.begin());
+      const auto at = index.find(d.host_nodes[k].slot[c]);
+      st[c] = at == index.end() ? kNotStaged : (uint16_t)at->second;
     }
     set_stage(k, st);
   }
@@ -530,8 +533,7 @@ void free_device(DeviceImage& d) {
   }
   d.ordered = false;
   d.top = nullptr;
-  d.top_keys.clear();
-  for (auto& c : d.top_count) c = 0;
+  for (auto& c : d.top_count) c = 0;  // top_keys describe the host mirror, which stays
   d.nodes = nullptr;
   d.voxels = d.vbits = d.colors = d.datas = nullptr;
   d.node_cap = d.brick_cap = d.color_cap = d.data_cap = 0;
@@ -556,12 +558,25 @@ svo_status full_upload(svo_scene* sc, cudaStream_t st, bool ordered = false) {
   d.data_cap = ndt + ndt / 4 + 64;
   const uint32_t W = vwords_of(t), len = t.arena.len();
   try {
-    d.host_nodes.assign(nn, DevNode{});
-    for (uint64_t k = 0; k < nn; ++k) build_node(t, k, d.host_nodes[k]);
+    // the host mirror of the records is rebuilt where the tree changed since it was last built (all of
+    // it the first time, or after svo_scene_release_device); a scene evicted by a server and uploaded
+    // again unchanged only copies
+    const bool reuse = d.mirror_ok && d.host_nodes.size() <= nn && d.host_vbits.size() <= t.arena.slots() * (size_t)W;
+    if (!reuse) {
+      d.host_nodes.assign(nn, DevNode{});
+      d.host_vbits.assign(t.arena.slots() * (size_t)W, 0u);
+    }
+    d.host_nodes.resize(nn);
+    d.host_vbits.resize(t.arena.slots() * (size_t)W, 0u);
+    auto& bd = t.arena.dirty();
+    for (uint64_t k = 0; k < nn; ++k)
+      if (!reuse || t.node_dirty[k]) build_node(t, k, d.host_nodes[k]);
+    for (uint32_t sl = 0; sl < t.arena.slots(); ++sl)
+      if (!reuse || bd[sl]) build_vbits(t, sl, &d.host_vbits[(size_t)sl * W]);
     stage_top(t, d);
-    d.host_vbits.assign(t.arena.slots() * (size_t)W, 0u);
-    for (uint32_t sl = 0; sl < t.arena.slots(); ++sl) build_vbits(t, sl, &d.host_vbits[(size_t)sl * W]);
+    d.mirror_ok = true;
   } catch (const ReferencePanic& p) {
+    d.mirror_ok = false;
     return fail(SVO_ERR_REFERENCE_PANIC, std::string("upload: ") + p.what());
   }
   {
@@ -895,8 +910,8 @@ svo_status evict_ordered(svo_scene* sc, cudaStream_t st) {
   d.node_cap = d.brick_cap = d.color_cap = d.data_cap = 0;
   d.valid = false;
   d.ordered = false;
-  std::fill(sc->tree.node_dirty.begin(), sc->tree.node_dirty.end(), 1);
-  std::fill(sc->tree.arena.dirty().begin(), sc->tree.arena.dirty().end(), 1);
+  // the host mirror and the dirty flags stay: uploading the scene again copies the mirror, after
+  // rebuilding what changed meanwhile
   return SVO_OK;
 }
 }  // namespace svo

@@ -81,7 +81,8 @@ struct DeviceImage {
   std::vector<uint32_t> top_keys;                 // node key of each top-table record
   std::vector<DevNode> host_top;                  // the records as uploaded
   bool valid = false;
-  bool ordered = false;  // image arrays from the stream-ordered pool (a server's residency)
+  bool ordered = false;    // image arrays from the stream-ordered pool (a server's residency)
+  bool mirror_ok = false;  // host_nodes / host_vbits / the top table match the tree but for dirty elements
   // host mirror of the node records and voxel bits (source of in-place syncs)
   std::vector<DevNode> host_nodes;
   std::vector<uint32_t> host_vbits;

@@ -165,6 +165,25 @@ svo_status make_resident(svo_server* sv, const std::vector<uint32_t>& need, size
   return SVO_OK;
 }
 
+// Evicts idle least-recently-used scenes while the resident images exceed the budget: an admission
+// goes over it when every resident scene is in use, and this brings residency back as launches
+// retire.  `st` is a stream with nothing in flight (a retired launch's).
+svo_status trim_residency(svo_server* sv, size_t n_scenes, cudaStream_t st, LaunchCounts& cnt) {
+  while (resident_bytes(sv, n_scenes) > sv->cfg.budget_bytes) {
+    int victim = -1;
+    for (size_t j = 0; j < n_scenes; ++j) {
+      const SceneSlot& c = sv->scenes[j];
+      if (!c.scene->dev.valid || c.users > 0) continue;
+      if (victim < 0 || c.last_used < sv->scenes[victim].last_used) victim = (int)j;
+    }
+    if (victim < 0) break;
+    svo_status rc = evict_ordered(sv->scenes[victim].scene, st);
+    if (rc != SVO_OK) return rc;
+    cnt.evictions++;
+  }
+  return SVO_OK;
+}
+
 svo_status launch(svo_server* sv, LaunchSlot& ls, size_t n_scenes, LaunchCounts& cnt) {
   TraceRange range("svo_server launch");
   uint64_t total = 0;
@@ -236,8 +255,10 @@ void worker_main(svo_server* sv) {
   for (;;) {
     bool progressed = false;
     // retire finished launches
+    cudaStream_t idle_stream = nullptr;
     for (LaunchSlot& ls : sv->slots) {
       if (!ls.busy || cudaEventQuery(ls.done) != cudaSuccess) continue;
+      idle_stream = ls.st;
       TraceRange range("svo_server retire");
       const double t = now_s();
       for (Request* q : ls.reqs) {
@@ -252,6 +273,14 @@ void worker_main(svo_server* sv) {
       ls.busy = false;
       progressed = true;
       sv->cv_done.notify_all();
+    }
+    if (idle_stream) {  // scenes admitted over the budget while all were in use leave as they go idle
+      const size_t n_scenes = sv->scenes.size();
+      LaunchCounts cnt;
+      lk.unlock();
+      trim_residency(sv, n_scenes, idle_stream, cnt);
+      lk.lock();
+      sv->stats.evictions += cnt.evictions;
     }
     // admit pending requests into free launch slots
     for (LaunchSlot& ls : sv->slots) {

@@ -110,3 +110,39 @@ def test_server_rejects_unknown_scene_and_reports_timeouts():
     with pytest.raises(RuntimeError):
         srv.wait(rid)  # a request is waited for once
     srv.close()
+
+
+def test_budget_pressure_evicts_and_trims_with_the_same_results():
+    """A budget of half the scene images: requests for six scenes keep evicting and uploading (in stream
+    order, on the launches' streams) while launches overlap; every result equals the plain cast, and once
+    the server is idle the resident images are back within the budget."""
+    sc = scenes() + scenes()[:3]
+    for j, t in enumerate(sc[3:]):  # three more scenes of their own
+        t.insert((j + 1, j + 2, j + 3), albedo=0x10203040 + j, user=77 + j)
+    images = []
+    for t in sc:
+        t.upload()
+        images.append(t.stats()["device_bytes"])
+        t.release_device()
+    budget = sum(images) // 2
+    reqs = requests(sc, np.random.default_rng(7), 120)
+    ref = [expected(sc, r) for r in reqs]
+    for t in sc:
+        t.release_device()
+    srv = svo.Server(budget_bytes=budget, max_batch_requests=4, max_inflight=3)
+    try:
+        ids = [srv.add_scene(t) for t in sc]
+        outs = [out_arrays(r[4], r[5]) for r in reqs]
+        rids = [srv.submit(*r, out=o) for r, o in zip(reqs, outs)]
+        for rid in rids:
+            srv.wait(rid, 120.0)
+        for o, e in zip(outs, ref):
+            same(o, e)
+        st = srv.stats()
+        assert st["evictions"] > 0 and st["uploads"] > len(ids)
+        deadline = srv.now() + 10.0
+        while srv.stats()["resident_bytes"] > budget and srv.now() < deadline:
+            pass  # the trim runs as the last launches retire
+        assert srv.stats()["resident_bytes"] <= budget
+    finally:
+        srv.close()
