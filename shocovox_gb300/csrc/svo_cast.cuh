@@ -777,9 +777,12 @@ __device__ void cast_ray_fast_from(const SceneView& s, const SharedLuts& L, floa
         continue;
       }
       Bounds tb = child_bounds(cb, target);
-      uint32_t ck = kind == kKindInternal ? (staged ? sn->slot[target] : __ldg(&nd->slot[target])) : kInvalidChild;
       if (kCount) h.creads++;
-      if (ck != kInvalidChild && (occ & L.octant[target]) != 0) {
+      // the child key is read only where the octant is occupied: an empty octant neither pushes nor
+      // stops an ADVANCE, whatever its key
+      uint32_t ck = kInvalidChild;
+      if (kind == kKindInternal && (occ & L.octant[target]) != 0) ck = staged ? sn->slot[target] : __ldg(&nd->slot[target]);
+      if (ck != kInvalidChild) {
         // PUSH (the child's octant in its parent rides along: 3 bits per stack entry); a staged
         // node's staged child is entered through its copy
         if (staged) {
@@ -811,7 +814,6 @@ __device__ void cast_ray_fast_from(const SceneView& s, const SharedLuts& L, floa
           target = step_fast(target, move, r.pos);
           if (target == kOob) break;
           tb = child_bounds(cb, target);
-          ck = kind == kKindInternal ? (staged ? sn->slot[target] : __ldg(&nd->slot[target])) : kInvalidChild;
           if (kCount) h.creads++;
           if (move & 1u) bx = bx + dbx;
           if (move & 4u) by = by + dby;
@@ -823,7 +825,10 @@ __device__ void cast_ray_fast_from(const SceneView& s, const SharedLuts& L, floa
             return;
           }
           flat = ux + 4u * uy + 16u * uz;
-          if (ck != kInvalidChild && (occ & L.octant[target]) != 0 && (rtn[flat * 8u] & occ) != 0) break;
+          if (kind == kKindInternal && (occ & L.octant[target]) != 0 && (rtn[flat * 8u] & occ) != 0) {
+            ck = staged ? sn->slot[target] : __ldg(&nd->slot[target]);
+            if (ck != kInvalidChild) break;
+          }
           if (kind == kKindLeaf && ((meta >> (8 + 2 * target)) & 3u) != kBkEmpty) break;
         }
       }

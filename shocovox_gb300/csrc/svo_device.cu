@@ -206,6 +206,9 @@ __global__ void __launch_bounds__(128, 7)
   __shared__ SharedLuts L;
   __shared__ WaitingRays waiting[4];
   __shared__ uint32_t in_flight[4];  // rays of each warp in flight (parked ones included)
+  // each thread's ray between two runs: 23 words a thread, an odd stride, so the 32 lanes of a warp
+  // touch 32 different banks; registers hold the state only while the ray runs
+  __shared__ FastState parked[128];
   extern __shared__ uint4 staged_smem[];
   DevNode* stg = reinterpret_cast<DevNode*>(staged_smem);
   fill_shared_luts(L);
@@ -219,7 +222,6 @@ __global__ void __launch_bounds__(128, 7)
   uint32_t park = park_below;
   bool alive = false;
   uint64_t i = 0;
-  FastState st;
   for (;;) {
     const unsigned idle = __ballot_sync(0xFFFFFFFFu, !alive);
     const uint32_t need = __popc(idle);
@@ -278,7 +280,7 @@ __global__ void __launch_bounds__(128, 7)
             write_hit(s, out, i, h);
             if (kCount) write_counters(out, i, h);
           } else {
-            fast_start(st, dx, dy, dz, px, py, pz, tg & 0x7FFFFFFFu);
+            fast_start(parked[threadIdx.x], dx, dy, dz, px, py, pz, tg & 0x7FFFFFFFu);
             alive = true;
           }
         }
@@ -295,11 +297,14 @@ __global__ void __launch_bounds__(128, 7)
       }
     }
     if (alive) {
+      FastState st = parked[threadIdx.x];
       HitRecord h;
       if (fast_run<kCount, kStage>(st, s, L, h, live, park, stg, stage_n)) {
         write_hit(s, out, i, h);
         if (kCount) write_counters(out, i, h);
         alive = false;
+      } else {
+        parked[threadIdx.x] = st;
       }
     }
     __syncwarp();

@@ -26,6 +26,7 @@ struct FastState {
   uint32_t cur, target, s0, s1, s2, s3, count, oct, work;
   uint32_t visits, creads, vreads, runs;
 };
+static_assert(sizeof(FastState) == 23 * 4, "23 words: an odd stride in shared memory");
 
 // Starts the state of a ray that entered the root at p in its octant `target` (fast_entry).
 __device__ __forceinline__ void fast_start(FastState& st, float dx, float dy, float dz, float px, float py, float pz,
@@ -165,9 +166,12 @@ __device__ __forceinline__ bool fast_run(FastState& st, const SceneView& s, cons
         continue;
       }
       Bounds tb = child_bounds(cb, target);
-      uint32_t ck = kind == kKindInternal ? (staged ? sn->slot[target] : __ldg(&nd->slot[target])) : kInvalidChild;
       if (kCount) h.creads++;
-      if (ck != kInvalidChild && (occ & L.octant[target]) != 0) {
+      // the child key is read only where the octant is occupied: an empty octant neither pushes nor
+      // stops an ADVANCE, whatever its key
+      uint32_t ck = kInvalidChild;
+      if (kind == kKindInternal && (occ & L.octant[target]) != 0) ck = staged ? sn->slot[target] : __ldg(&nd->slot[target]);
+      if (ck != kInvalidChild) {
         // PUSH
         if (staged) {
           const uint32_t si = sn->stage[target];
@@ -199,7 +203,6 @@ __device__ __forceinline__ bool fast_run(FastState& st, const SceneView& s, cons
           target = step_fast(target, move, r.pos);
           if (target == kOob) break;
           tb = child_bounds(cb, target);
-          ck = kind == kKindInternal ? (staged ? sn->slot[target] : __ldg(&nd->slot[target])) : kInvalidChild;
           if (kCount) h.creads++;
           if (move & 1u) bx = bx + dbx;
           if (move & 4u) by = by + dby;
@@ -211,7 +214,10 @@ __device__ __forceinline__ bool fast_run(FastState& st, const SceneView& s, cons
             break;
           }
           flat = ux + 4u * uy + 16u * uz;
-          if (ck != kInvalidChild && (occ & L.octant[target]) != 0 && (rtn[flat * 8u] & occ) != 0) break;
+          if (kind == kKindInternal && (occ & L.octant[target]) != 0 && (rtn[flat * 8u] & occ) != 0) {
+            ck = staged ? sn->slot[target] : __ldg(&nd->slot[target]);
+            if (ck != kInvalidChild) break;
+          }
           if (kind == kKindLeaf && ((meta >> (8 + 2 * target)) & 3u) != kBkEmpty) break;
         }
         st.target = target;
