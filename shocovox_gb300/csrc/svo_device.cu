@@ -297,14 +297,11 @@ __global__ void __launch_bounds__(128, 7)
       }
     }
     if (alive) {
-      FastState st = parked[threadIdx.x];
       HitRecord h;
-      if (fast_run<kCount, kStage>(st, s, L, h, live, park, stg, stage_n)) {
+      if (fast_run<kCount, kStage>(parked + threadIdx.x, s, L, h, live, park, stg, stage_n)) {
         write_hit(s, out, i, h);
         if (kCount) write_counters(out, i, h);
         alive = false;
-      } else {
-        parked[threadIdx.x] = st;
       }
     }
     __syncwarp();

@@ -46,18 +46,23 @@ __device__ __forceinline__ void fast_start(FastState& st, float dx, float dy, fl
 // Runs the ray until it is done (true: `h` holds its record) or parks at a node visit (false) because
 // `*live` (rays of the warp still in flight) fell below park_below (0: never park).  A ray that ends
 // decrements *live.
+// The ray's state stays in its slot `ps` (shared memory) between runs: a run reads it, keeps it in
+// registers while the ray moves, and writes back only what changed when the ray parks.
 template <bool kCount, bool kStage = false>
-__device__ __forceinline__ bool fast_run(FastState& st, const SceneView& s, const SharedLuts& L, HitRecord& h,
+__device__ __forceinline__ bool fast_run(FastState* ps, const SceneView& s, const SharedLuts& L, HitRecord& h,
                                          volatile uint32_t* live, uint32_t park_below, const DevNode* stg = nullptr,
                                          uint32_t stg_n = 0) {
   miss_record(h);
+  struct {
+    uint32_t cur, target, s0, s1, s2, s3, count, oct, work;
+  } st = {ps->cur, ps->target, ps->s0, ps->s1, ps->s2, ps->s3, ps->count, ps->oct, ps->work};
   FastRay r;
-  r.dx = st.dx;
-  r.dy = st.dy;
-  r.dz = st.dz;
-  r.px = st.px;
-  r.py = st.py;
-  r.pz = st.pz;
+  r.dx = ps->dx;
+  r.dy = ps->dy;
+  r.dz = ps->dz;
+  r.px = ps->px;
+  r.py = ps->py;
+  r.pz = ps->pz;
   r.pos = (rsignum(r.dx) > 0.0f ? 1u : 0u) | (rsignum(r.dz) > 0.0f ? 2u : 0u) | (rsignum(r.dy) > 0.0f ? 4u : 0u);
   {  // get_dda_scale_factors (raytracing_on_cpu.rs:99-112); powf(q, 2.) == q * q
     const float a = r.dz / r.dx, b = r.dy / r.dx, c = r.dx / r.dy, d = r.dz / r.dy, e = r.dx / r.dz, f = r.dy / r.dz;
@@ -66,13 +71,13 @@ __device__ __forceinline__ bool fast_run(FastState& st, const SceneView& s, cons
     r.fz = sqrtf((e * e + 1.0f) + f * f);
   }
   if (kCount) {
-    h.visits = st.visits;
-    h.creads = st.creads;
-    h.vreads = st.vreads;
-    h.runs = st.runs;
+    h.visits = ps->visits;
+    h.creads = ps->creads;
+    h.vreads = ps->vreads;
+    h.runs = ps->runs;
   }
   // node bounds: sizes are powers of two, so 1 / size is exact
-  Bounds cb{st.bx, st.by, st.bz, st.bs, st.count ? 1.0f / st.bs : 0.0f};
+  Bounds cb{ps->bx, ps->by, ps->bz, ps->bs, st.count ? 1.0f / ps->bs : 0.0f};
   const float g4x = (r.pos & 1u) ? 4.0f : -4.0f, g4y = (r.pos & 4u) ? 4.0f : -4.0f, g4z = (r.pos & 2u) ? 4.0f : -4.0f;
   const uint32_t dir = hash_region(1.0f + r.dx, 1.0f + r.dy, 1.0f + r.dz, 1.0f);
   const uint64_t* rtn = L.ray_to_node + dir;
@@ -94,18 +99,27 @@ __device__ __forceinline__ bool fast_run(FastState& st, const SceneView& s, cons
     }
     while (st.count > 0) {
       if (park_below && *live < park_below) {  // parked at the top of a node visit
-        st.px = r.px;
-        st.py = r.py;
-        st.pz = r.pz;
-        st.bx = cb.x;
-        st.by = cb.y;
-        st.bz = cb.z;
-        st.bs = cb.s;
+        ps->px = r.px;
+        ps->py = r.py;
+        ps->pz = r.pz;
+        ps->bx = cb.x;
+        ps->by = cb.y;
+        ps->bz = cb.z;
+        ps->bs = cb.s;
+        ps->cur = st.cur;
+        ps->target = st.target;
+        ps->s0 = st.s0;
+        ps->s1 = st.s1;
+        ps->s2 = st.s2;
+        ps->s3 = st.s3;
+        ps->count = st.count;
+        ps->oct = st.oct;
+        ps->work = st.work;
         if (kCount) {
-          st.visits = h.visits;
-          st.creads = h.creads;
-          st.vreads = h.vreads;
-          st.runs = h.runs;
+          ps->visits = h.visits;
+          ps->creads = h.creads;
+          ps->vreads = h.vreads;
+          ps->runs = h.runs;
         }
         return false;
       }
