@@ -369,7 +369,7 @@ def autotune_batched(svo, torch, ws, items, stream, fixed_sort=None):
 
 def cfg_record(c):
     return {"block": c.block, "rays_per_chunk": c.rays_per_chunk, "block_shape": c.block_shape, "sort_key": c.sort_key,
-            "staging_depth": c.staging_depth}
+            "staging_depth": c.staging_depth, "refill_below": c.refill_below}
 
 
 # ---- single scene: terrain512 (default), heightfield128, incoherent1024 ----------------------------

@@ -298,6 +298,10 @@ typedef struct {
   uint32_t staging_depth;  /* top tree levels staged in shared memory by every block: the Internal nodes of
                               depth < staging_depth (0..4) of each scene of the call, as far as 48 KB of
                               records per block reach (scenes past that read their nodes from L1/L2) */
+  uint32_t refill_below;   /* with sort_key 1: the sorted rays' cast parks a warp's rays at a node visit once
+                              fewer than refill_below (1..32) are in flight, gives its idle lanes the next
+                              sorted rays and resumes (see svo_set_refill); 0 = each warp's rays run to
+                              their ends.  The hits are the same for every value. */
 } svo_launch_config;
 
 /* Casts every item's rays in one persistent kernel launch driven by a device

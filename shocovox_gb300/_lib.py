@@ -54,7 +54,8 @@ class SceneRecipe(ctypes.Structure):
 
 class LaunchConfig(ctypes.Structure):
     _fields_ = [("block", ctypes.c_uint32), ("rays_per_chunk", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32),
-                ("block_shape", ctypes.c_uint32), ("sort_key", ctypes.c_uint32), ("staging_depth", ctypes.c_uint32)]
+                ("block_shape", ctypes.c_uint32), ("sort_key", ctypes.c_uint32), ("staging_depth", ctypes.c_uint32),
+                ("refill_below", ctypes.c_uint32)]
 
 
 class ServerConfig(ctypes.Structure):

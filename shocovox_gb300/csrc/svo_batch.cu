@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "svo_cast.cuh"
+#include "svo_refill.cuh"
 #include "svo_trace.h"
 
 namespace svo {
@@ -592,6 +593,96 @@ __global__ void __launch_bounds__(kBatchMaxBlock, 7)
   }
 }
 
+// The sorted cast with lane refill (svo_launch_config.refill_below): a warp parks its rays at a node
+// visit once fewer than park_below are in flight (refill_kernel, svo_device.cu) and its idle lanes
+// take the next sorted records, claimed exactly as many as there are idle lanes, so the list's order
+// (neighbouring entry points, one direction octant) carries over into the refilled warp.
+template <bool kCount, bool kOne, bool kStage = false>
+__global__ void __launch_bounds__(kBatchMaxBlock, 7)
+    sorted_refill_kernel(const BatchItemDev* __restrict__ items, const SortedRay* __restrict__ sorted,
+                         const unsigned long long* __restrict__ n_list, unsigned long long* __restrict__ counter,
+                         const SceneView one_scene, const HitsView one_hits, uint32_t n_items, uint32_t one_stage_n,
+                         uint32_t park_below) {
+  __shared__ SharedLuts L;
+  __shared__ uint32_t in_flight[kBatchMaxBlock / 32];
+  __shared__ FastState parked[kBatchMaxBlock];  // a thread's ray between runs (23 words: no bank conflicts)
+  extern __shared__ uint4 staged_smem[];
+  DevNode* stg = reinterpret_cast<DevNode*>(staged_smem);
+  fill_shared_luts(L);
+  if (kStage) {
+    if (kOne)
+      stage_records(stg, one_scene.top, one_stage_n);
+    else
+      stage_items(stg, items, n_items);
+  }
+  __syncthreads();
+  const uint64_t n = *n_list;
+  const uint32_t lane = threadIdx.x & 31u;
+  volatile uint32_t* live = in_flight + (threadIdx.x >> 5);
+  uint32_t park = park_below;
+  bool more = true, alive = false;
+  uint64_t i = 0;    // the ray's index in its item
+  uint32_t item = 0;
+  for (;;) {
+    const unsigned idle = __ballot_sync(0xFFFFFFFFu, !alive);
+    const uint32_t need = __popc(idle);
+    if (need && more) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(counter, (unsigned long long)need);
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      if (base + need >= n) more = false;
+      if (!alive) {
+        const uint64_t k = base + __popc(idle & ((1u << lane) - 1u));
+        if (k < n) {
+          const float4* src = reinterpret_cast<const float4*>(sorted + k);
+          const float4 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2), d = __ldg(src + 3);
+          const uint32_t target = __float_as_uint(c.y);
+          i = (uint64_t)__float_as_uint(d.z) | ((uint64_t)__float_as_uint(d.w) << 32);
+          item = kOne ? 0u : __float_as_uint(c.z);
+          if ((target >> 31) == 0u) {  // a NaN direction (or literal mode): the literal form, in one go
+            HitRecord h;
+            const SceneView& sc = kOne ? one_scene : items[item].scene;
+            const HitsView& hv = kOne ? one_hits : items[item].hits;
+            cast_entered<kCount>(sc, L, a.x, a.y, a.z, a.w, b.x, b.y, false, b.z, b.w, c.x, 0u, h);
+            write_hit(sc, hv, i, h);
+            if (kCount) write_counters(hv, i, h);
+          } else {
+            fast_start(parked[threadIdx.x], a.w, b.x, b.y, b.z, b.w, c.x, target & 0x7FFFFFFFu);
+            alive = true;
+          }
+        }
+      }
+      if (!more) park = 0;  // nothing left to hand out: rays in flight run to their end
+      __syncwarp();
+      const unsigned now = __ballot_sync(0xFFFFFFFFu, alive);
+      if (lane == 0) *live = __popc(now);
+      __syncwarp();
+      if (now == 0) continue;
+    } else if (!__any_sync(0xFFFFFFFFu, alive)) {
+      break;
+    }
+    if (alive) {
+      HitRecord h;
+      if (kOne) {
+        if (fast_run<kCount, kStage>(parked + threadIdx.x, one_scene, L, h, live, park, stg, one_stage_n)) {
+          write_hit(one_scene, one_hits, i, h);
+          if (kCount) write_counters(one_hits, i, h);
+          alive = false;
+        }
+      } else {
+        const BatchItemDev& it = items[item];
+        if (fast_run<kCount, kStage>(parked + threadIdx.x, it.scene, L, h, live, park, stg + it.stage_off,
+                                     it.stage_n)) {
+          write_hit(it.scene, it.hits, i, h);
+          if (kCount) write_counters(it.hits, i, h);
+          alive = false;
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
 }  // namespace svo
 
 namespace svo {
@@ -713,6 +804,11 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
   if (shape < 3 || shape > 5) return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: block_shape must be 0, 3, 4 or 5");
   const uint32_t sort_key = cfg ? cfg->sort_key : 0;
   if (sort_key > 1) return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: sort_key must be 0 or 1");
+  const uint32_t depth = cfg ? cfg->staging_depth : 0;
+  if (depth > kMaxStageDepth)
+    return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: staging_depth must be 0.." + std::to_string(kMaxStageDepth));
+  const uint32_t refill = cfg ? cfg->refill_below : 0;
+  if (refill > 32) return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: refill_below must be 0..32");
   uint64_t total = 0, sort_total = 0, buckets = 0;
   bool count = false;
   for (uint32_t i = 0; i < n_items; ++i) {
@@ -737,9 +833,6 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
   if (total == 0 && sort_total == 0) return SVO_OK;
   if (sort_total >= (1ull << 32) || buckets >= (1ull << 32))
     return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: the ray sort takes fewer than 2^32 rays per call");
-  const uint32_t depth = cfg ? cfg->staging_depth : 0;
-  if (depth > kMaxStageDepth)
-    return fail(SVO_ERR_ARGUMENT, "svo_cast_batched: staging_depth must be 0.." + std::to_string(kMaxStageDepth));
   const uint32_t staged_n = assign_staging(ws->h_items, items, n_items, depth);
   const size_t stage_smem = (size_t)staged_n * sizeof(DevNode);
   const uint32_t block = (cfg && cfg->block) ? cfg->block : 128;
@@ -812,6 +905,23 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
     const uint32_t one_stage = single ? ws->h_items[one.index].stage_n : 0u;
     const bool stage = single ? one_stage > 0 : staged_n > 0;
     const size_t smem = single ? (size_t)one_stage * sizeof(DevNode) : stage_smem;
+    if (refill) {
+      auto rk = stage ? (single ? (count ? sorted_refill_kernel<true, true, true> : sorted_refill_kernel<false, true, true>)
+                                : (count ? sorted_refill_kernel<true, false, true> : sorted_refill_kernel<false, false, true>))
+                      : (single ? (count ? sorted_refill_kernel<true, true> : sorted_refill_kernel<false, true>)
+                                : (count ? sorted_refill_kernel<true, false> : sorted_refill_kernel<false, false>));
+      SVO_CUDA_TRY(allow_dynamic_smem(rk, smem));
+      int per_sm = (cfg && cfg->blocks_per_sm) ? (int)cfg->blocks_per_sm : 0;
+      if (per_sm == 0) {
+        SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rk, block, smem));
+        per_sm = std::max(per_sm, 1);
+      }
+      uint64_t grid = (uint64_t)ws->sm_count * (uint64_t)per_sm;
+      grid = std::max<uint64_t>(1, std::min<uint64_t>(grid, (sort_total + block - 1) / block));
+      rk<<<(unsigned)grid, block, smem, st>>>(ws->d_items, ws->d_sorted, n_list, ws->d_counter, one.scene, one.hits,
+                                               n_items, one_stage, refill);
+      SVO_CUDA_TRY(cudaGetLastError());
+    } else {
     auto cast = stage ? (single ? (count ? sorted_cast_kernel<true, true, true> : sorted_cast_kernel<false, true, true>)
                                 : (count ? sorted_cast_kernel<true, false, true> : sorted_cast_kernel<false, false, true>))
                       : (single ? (count ? sorted_cast_kernel<true, true> : sorted_cast_kernel<false, true>)
@@ -828,6 +938,7 @@ svo_status svo_cast_batched(svo_batch_workspace* ws, const svo_batch_item* items
     cast<<<(unsigned)grid, block, smem, st>>>(ws->d_items, ws->d_sorted, n_list, ws->d_counter, chunk, one.scene,
                                                one.hits, n_items, one_stage);
     SVO_CUDA_TRY(cudaGetLastError());
+    }
   }
   if (total == 0) return SVO_OK;
   return launch_claimed(ws->d_items, n_items, total, ws->d_counter, chunk, block, cfg, count, staged_n, ws->sm_count, st);

@@ -21,15 +21,16 @@ def items_of(*specs):
     return [(FakeScene(s, d), {}, n, {}, row) for s, d, n, row in specs]
 
 
-def fake_time(best, best_stage=0):
+def fake_time(best, best_stage=0, best_refill=0):
     seen = []
 
     def time_fn(cfg):
         key = (cfg.block, cfg.rays_per_chunk, cfg.blocks_per_sm, cfg.block_shape, cfg.sort_key)
-        seen.append(key + (cfg.staging_depth,))
+        seen.append(key + (cfg.staging_depth, cfg.refill_below))
         if key != best:
             return 2.0 + 0.001 * len(seen)
-        return 1.0 - 0.1 * (cfg.staging_depth == best_stage)  # the best knobs, fastest at depth best_stage
+        # the best knobs: fastest at depth best_stage, and with refill best_refill (when not 0)
+        return 1.0 - 0.1 * (cfg.staging_depth == best_stage) - 0.05 * (best_refill and cfg.refill_below == best_refill)
 
     return time_fn, seen
 
@@ -48,13 +49,16 @@ def test_sweep_covers_the_knobs_of_the_batch(rows, want_shapes, want_sorts):
     assert {k[4] for k in seen} == want_sorts
     assert {k[0] for k in seen} == set(autotune.BLOCKS) and {k[1] for k in seen} == set(autotune.CHUNKS)
     first = len(autotune.BLOCKS) * len(autotune.CHUNKS) * len(want_shapes) * len(want_sorts)
-    assert len(seen) == len(set(seen)) == first + len(autotune.STAGING)
-    assert all(k[5] == 0 for k in seen[:first])  # the first stage at staging depth 0
-    assert [k[:5] for k in seen[first:]] == [best] * len(autotune.STAGING)  # then the depths on the best
-    assert {k[5] for k in seen[first:]} == set(autotune.STAGING)
+    refills = len(autotune.REFILL) if best[4] == 1 else 0  # the refill stage only for a sorted best
+    assert len(seen) == len(set(seen)) == first + len(autotune.STAGING) + refills
+    assert all(k[5] == 0 and k[6] == 0 for k in seen[:first])  # the first stage: nothing staged, no refill
+    stage = seen[first:first + len(autotune.STAGING)]
+    assert [k[:5] for k in stage] == [best] * len(autotune.STAGING)  # then the depths on the best
+    assert {k[5] for k in stage} == set(autotune.STAGING) and all(k[6] == 0 for k in stage)
+    assert {k[6] for k in seen[first + len(autotune.STAGING):]} == (set(autotune.REFILL) if refills else set())
     assert (cfg.block, cfg.rays_per_chunk, cfg.blocks_per_sm, cfg.block_shape, cfg.sort_key) == best
-    assert cfg.staging_depth == 0
-    assert info["cached"] is False and info["config"] == list(best) + [0]
+    assert cfg.staging_depth == 0 and cfg.refill_below == 0
+    assert info["cached"] is False and info["config"] == list(best) + [0, 0]
 
 
 @pytest.mark.parametrize("depth", [0, 2, 4])
@@ -64,6 +68,19 @@ def test_staging_depth_is_kept_only_when_faster(depth):
     time_fn, seen = fake_time(best, best_stage=depth)
     cfg, info = autotune.tune(None, items, "gpu", time_fn, use_cache=False)
     assert cfg.staging_depth == depth and info["config"][5] == depth
+
+
+@pytest.mark.parametrize("refill", [0, 24])
+def test_refill_is_swept_for_the_sorted_cast(refill):
+    items = items_of((1024, 8, 4_000_000, 0))
+    best = (128, 32, 0, 0, 1)
+    time_fn, seen = fake_time(best, best_stage=0, best_refill=refill)
+    cfg, info = autotune.tune(None, items, "gpu", time_fn, use_cache=False)
+    assert cfg.sort_key == 1 and cfg.refill_below == refill and info["config"][6] == refill
+    # refill is tried only with the sort
+    time_fn, seen = fake_time((128, 32, 0, 0, 0))
+    autotune.tune(None, items, "gpu", time_fn, use_cache=False)
+    assert {k[6] for k in seen} == {0}
 
 
 def test_empty_items_do_not_ask_for_the_sort():
@@ -91,7 +108,7 @@ def test_cache_round_trip_and_older_entries(tmp_path, monkeypatch):
     # an entry with four knobs (no sort key, no staging depth) reads as index order, nothing staged
     with open(autotune.CACHE) as f:
         cache = json.load(f)
-    key = "GB300|%s|stage" % autotune.signature(items)
+    key = "GB300|%s|refill" % autotune.signature(items)
     cache[key]["config"] = [64, 128, 0, 4]
     with open(autotune.CACHE, "w") as f:
         json.dump(cache, f)
@@ -117,3 +134,4 @@ def test_launch_count_of_a_batched_call():
     assert bench.batched_launches([cam, empty], 1) == 1
     assert LaunchConfig(1, 2, 3, 4, 1).sort_key == 1 and LaunchConfig().sort_key == 0
     assert LaunchConfig(1, 2, 3, 4, 1, 3).staging_depth == 3 and LaunchConfig().staging_depth == 0
+    assert LaunchConfig(1, 2, 3, 4, 1, 3, 24).refill_below == 24 and LaunchConfig().refill_below == 0

@@ -67,3 +67,44 @@ def test_refill_is_checked():
     assert svo.lib().svo_set_refill(33) == 6
     assert svo.lib().svo_set_refill(-1) == 6
     assert svo.lib().svo_set_refill(0) == 0
+
+
+@pytest.mark.parametrize("n_items", [1, 4])
+@pytest.mark.parametrize("refill", [8, 24, 32])
+def test_sorted_batched_cast_with_refill(oracle_mod, n_items, refill):
+    """svo_launch_config.refill_below on the ray sort's cast: one sorted item (its views in the kernel
+    parameters) and several, staged top levels or not, counters included."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    tmap = {np.uint8: torch.uint8, np.uint32: torch.int32, np.float32: torch.float32}
+    rng = np.random.default_rng(40 + n_items)
+    items, refs, outs = [], [], []
+    for j, (kind, size, dim) in enumerate([(2, 512, 8), (3, 128, 2), (0, 128, 4), (1, 64, 8)][:n_items]):
+        ops = svo.gen_scene(kind, size, dim, seed=90 + j, occupancy=0.06, spheres=3, octaves=2, base_freq=1.0 / 16,
+                            height_lo=2.0, height_hi=size * 0.35)
+        o, p = both(oracle_mod, size, dim, ops)
+        so, sd = svo.gen_sphere_rays([size / 2] * 3, size * np.sqrt(3.0) / 2, 40_000, 3 + j)
+        ro, rd = random_rays(rng, size, 4_000)
+        a, b = np.concatenate([so, ro]), np.concatenate([sd, rd])
+        refs.append(o.cast(a, b))
+        r = {k: torch.from_numpy(np.ascontiguousarray(arr[:, i])).to(dev)
+             for arr, ks in ((a, ("ox", "oy", "oz")), (b, ("dx", "dy", "dz"))) for i, k in enumerate(ks)}
+        out = {k: torch.zeros(len(a), dtype=tmap[t], device=dev) for k, t in svo.HIT_FIELDS.items()}
+        outs.append((out, r, len(a)))
+        items.append((p, {k: v.data_ptr() for k, v in r.items()}, len(a), {k: v.data_ptr() for k, v in out.items()}, 0))
+    ws = svo.BatchWorkspace()
+    for depth in (0, 2):
+        ws.cast(items, svo.LaunchConfig(128, 32, 0, 0, 1, depth, refill), 0)
+        torch.cuda.synchronize()
+        for j, ((out, _, n), ref) in enumerate(zip(outs, refs)):
+            got = {k: v[:n].cpu().numpy().view(svo.HIT_FIELDS[k]) for k, v in out.items()}
+            assert_same_hits(got, ref, counters=True, label="item %d refill %d depth %d" % (j, refill, depth))
+
+
+def test_batched_refill_is_checked():
+    p = svo.Octree(64, 4)
+    p.insert((1, 1, 1), albedo=0xFF)
+    p.upload()
+    with pytest.raises(RuntimeError):
+        svo.BatchWorkspace().cast([(p, {k: 0 for k in ("ox", "oy", "oz", "dx", "dy", "dz")}, 0, {}, 0)],
+                                  svo.LaunchConfig(128, 32, 0, 0, 1, 0, 33), 0)
