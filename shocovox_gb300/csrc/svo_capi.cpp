@@ -269,12 +269,7 @@ svo_status svo_scene_stats_get(svo_scene* s, svo_scene_stats* out) {
   out->datas = t.datas.size();
   out->size = t.size;
   out->brick_dim = t.dim;
-  if (s->dev.valid) {
-    const DeviceImage& d = s->dev;
-    out->device_bytes = d.node_cap * sizeof(DevNode) + d.brick_cap * (uint64_t)t.arena.len() * 4 +
-                        d.brick_cap * (uint64_t)(t.arena.len() >= 32 ? t.arena.len() / 32 : 1) * 4 +
-                        (d.color_cap + d.data_cap) * 4;
-  }
+  out->device_bytes = device_image_bytes(s);  // what a server counts against its budget
   return SVO_OK;
 }
 

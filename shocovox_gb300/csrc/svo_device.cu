@@ -514,11 +514,26 @@ svo_status upload_top(DeviceImage& d, cudaStream_t st) {
   return SVO_OK;
 }
 
+void free_blob(DeviceImage& d) {
+  if (d.blob_done) {
+    cudaEventSynchronize(d.blob_done);  // no copy still reads the blob
+    cudaEventDestroy(d.blob_done);
+    d.blob_done = nullptr;
+  }
+  if (d.blob) cudaFreeHost(d.blob);
+  d.blob = nullptr;
+  d.blob_bytes = 0;
+  d.blob_ok = false;
+}
+
 void free_device(DeviceImage& d) {
   // cudaFree waits for no cast on memory from the stream-ordered pool: wait for the device here, as
   // cudaFree does for other memory, so that releasing a scene keeps the same meaning either way
-  if (d.ordered && (d.top || d.nodes)) cudaDeviceSynchronize();
-  if (d.ordered) {
+  if (d.ordered && (d.top || d.nodes || d.block)) cudaDeviceSynchronize();
+  if (d.block) {
+    cudaFree(d.block);
+    d.block = nullptr;
+  } else if (d.ordered) {
     cudaFree(d.top);
     cudaFree(d.nodes);
     cudaFree(d.voxels);
@@ -542,6 +557,100 @@ void free_device(DeviceImage& d) {
   d.valid = false;
 }
 
+// The tree has changed in nothing since the device image was last made or synced.
+bool tree_clean(HostOctree& t) {
+  auto none = [](const std::vector<uint8_t>& f) { return std::find(f.begin(), f.end(), 1) == f.end(); };
+  return !t.structure_grew && t.colors_synced == t.colors.size() && t.datas_synced == t.datas.size() &&
+         none(t.node_dirty) && none(t.arena.dirty());
+}
+
+// Marks the device image in step with the tree.
+void image_synced(HostOctree& t, DeviceImage& d) {
+  d.n_nodes = t.nodes();
+  d.n_bricks = t.arena.slots();
+  d.n_colors = t.colors.size();
+  d.n_datas = t.datas.size();
+  std::fill(t.node_dirty.begin(), t.node_dirty.end(), 0);
+  std::fill(t.arena.dirty().begin(), t.arena.dirty().end(), 0);
+  t.colors_synced = t.colors.size();
+  t.datas_synced = t.datas.size();
+  t.structure_grew = false;
+  d.valid = true;
+}
+
+// The stream-ordered image of a server's scene: one block of the pool, filled from the pinned blob
+// (the arrays in the order nodes, top table, voxels, voxel bits, colors, user data; each at a
+// 256-byte boundary).  `fill`: the host mirror changed, copy it into the blob first.
+svo_status upload_block(svo_scene* sc, cudaStream_t st, bool fill) {
+  HostOctree& t = sc->tree;
+  DeviceImage& d = sc->dev;
+  const uint64_t W = vwords_of(t), len = t.arena.len(), nb = t.arena.slots();
+  const uint64_t cap[6] = {d.node_cap * sizeof(DevNode), kMaxStaged * sizeof(DevNode), d.brick_cap * len * 4,
+                           d.brick_cap * W * 4, d.color_cap * 4, d.data_cap * 4};
+  uint64_t off[6], total = 0;
+  for (int i = 0; i < 6; ++i) {
+    off[i] = total;
+    total += (cap[i] + 255) / 256 * 256;
+  }
+  if (!fill && d.blob_bytes != total) {
+    stage_top(t, d);  // the top table of the (unchanged) mirror, for the blob made again below
+    fill = true;
+  }
+  if (fill) {
+    if (d.blob_bytes != total) {
+      free_blob(d);
+      void* h = nullptr;
+      if (cudaMallocHost(&h, total) != cudaSuccess) {
+        cudaGetLastError();
+        d.ordered = false;
+        free_device(d);
+        return fail(SVO_ERR_OUT_OF_MEMORY, "scene image: no pinned host memory for the upload copy");
+      }
+      d.blob = static_cast<uint8_t*>(h);
+      d.blob_bytes = total;
+    } else if (d.blob_done) {
+      SVO_CUDA_TRY(cudaEventSynchronize(d.blob_done));  // the last upload has finished reading the blob
+    }
+    d.host_top.resize(d.top_keys.size());
+    for (size_t i = 0; i < d.top_keys.size(); ++i) d.host_top[i] = d.host_nodes[d.top_keys[i]];
+    const void* src[6] = {d.host_nodes.data(), d.host_top.data(), t.arena.raw().data(), d.host_vbits.data(),
+                          t.colors.data(), t.datas.data()};
+    const uint64_t used[6] = {d.host_nodes.size() * sizeof(DevNode), d.host_top.size() * sizeof(DevNode),
+                              nb * len * 4, nb * W * 4, t.colors.size() * 4, t.datas.size() * 4};
+    for (int i = 0; i < 6; ++i)
+      if (used[i]) std::memcpy(d.blob + off[i], src[i], used[i]);
+    for (uint32_t k = 0; k <= kMaxStageDepth; ++k) d.blob_top_count[k] = d.top_count[k];
+    d.blob_ok = true;
+  } else {
+    for (uint32_t k = 0; k <= kMaxStageDepth; ++k) d.top_count[k] = d.blob_top_count[k];
+  }
+  void* p = nullptr;
+  {
+    const svo_status rc = image_alloc(&p, total, st, true);
+    if (rc != SVO_OK) {
+      d.ordered = false;
+      free_device(d);
+      return rc;
+    }
+  }
+  uint8_t* base = static_cast<uint8_t*>(p);
+  d.block = p;
+  d.nodes = reinterpret_cast<DevNode*>(base + off[0]);
+  d.top = reinterpret_cast<DevNode*>(base + off[1]);
+  d.voxels = reinterpret_cast<uint32_t*>(base + off[2]);
+  d.vbits = reinterpret_cast<uint32_t*>(base + off[3]);
+  d.colors = reinterpret_cast<uint32_t*>(base + off[4]);
+  d.datas = reinterpret_cast<uint32_t*>(base + off[5]);
+  const uint64_t used[6] = {t.nodes() * sizeof(DevNode), d.host_top.size() * sizeof(DevNode), nb * len * 4,
+                            nb * W * 4, t.colors.size() * 4, t.datas.size() * 4};
+  for (int i = 0; i < 6; ++i)
+    if (used[i]) SVO_CUDA_TRY(cudaMemcpyAsync(base + off[i], d.blob + off[i], used[i], cudaMemcpyHostToDevice, st));
+  if (!d.blob_done) SVO_CUDA_TRY(cudaEventCreateWithFlags(&d.blob_done, cudaEventDisableTiming));
+  SVO_CUDA_TRY(cudaEventRecord(d.blob_done, st));
+  image_synced(t, d);
+  return SVO_OK;
+}
+
 svo_status full_upload(svo_scene* sc, cudaStream_t st, bool ordered = false) {
   HostOctree& t = sc->tree;
   DeviceImage& d = sc->dev;
@@ -559,6 +668,9 @@ svo_status full_upload(svo_scene* sc, cudaStream_t st, bool ordered = false) {
   d.color_cap = nc + nc / 4 + 64;
   d.data_cap = ndt + ndt / 4 + 64;
   const uint32_t W = vwords_of(t), len = t.arena.len();
+  // a server's scene evicted and uploaded again unchanged: the blob already holds its image
+  if (d.ordered && d.blob_ok && d.mirror_ok && tree_clean(t)) return upload_block(sc, st, false);
+  if (!d.ordered) d.blob_ok = false;  // in-place syncs of this image do not reach the blob
   try {
     // the host mirror of the records is rebuilt where the tree changed since it was last built (all of
     // it the first time, or after svo_scene_release_device); a scene evicted by a server and uploaded
@@ -579,8 +691,10 @@ svo_status full_upload(svo_scene* sc, cudaStream_t st, bool ordered = false) {
     d.mirror_ok = true;
   } catch (const ReferencePanic& p) {
     d.mirror_ok = false;
+    d.blob_ok = false;
     return fail(SVO_ERR_REFERENCE_PANIC, std::string("upload: ") + p.what());
   }
+  if (d.ordered) return upload_block(sc, st, true);
   {
     // a failed allocation releases what the upload holds: the scene is left without a device image
     void* p[5] = {};
@@ -625,16 +739,7 @@ svo_status full_upload(svo_scene* sc, cudaStream_t st, bool ordered = false) {
     SVO_CUDA_TRY(cudaMemcpyAsync(d.datas, t.datas.data(), t.datas.size() * 4, cudaMemcpyHostToDevice, st));
   // pageable sources: the copies are staged before cudaMemcpyAsync returns, but
   // the mirrors must stay valid until then, which they do (they live in the scene)
-  d.n_nodes = nn;
-  d.n_bricks = t.arena.slots();
-  d.n_colors = t.colors.size();
-  d.n_datas = t.datas.size();
-  std::fill(t.node_dirty.begin(), t.node_dirty.end(), 0);
-  std::fill(t.arena.dirty().begin(), t.arena.dirty().end(), 0);
-  t.colors_synced = t.colors.size();
-  t.datas_synced = t.datas.size();
-  t.structure_grew = false;
-  d.valid = true;
+  image_synced(t, d);
   return SVO_OK;
 }
 
@@ -663,6 +768,7 @@ svo_status incremental_sync(svo_scene* sc, cudaStream_t st) {
   if (nn > d.node_cap || t.arena.slots() > d.brick_cap || t.colors.size() > d.color_cap || t.datas.size() > d.data_cap)
     return full_upload(sc, st);
   const uint32_t W = vwords_of(t), len = t.arena.len();
+  if (!tree_clean(t)) d.blob_ok = false;  // the image changes in place, the blob keeps the old one
   try {
     d.host_nodes.resize(nn);
     for (uint64_t k = 0; k < nn; ++k)
@@ -902,18 +1008,22 @@ svo_status evict_ordered(svo_scene* sc, cudaStream_t st) {
   TraceRange range("svo_scene_evict");
   DeviceImage& d = sc->dev;
   if (!d.ordered) return svo_scene_release_device(sc);
-  void* arrays[6] = {d.top, d.nodes, d.voxels, d.vbits, d.colors, d.datas};
-  for (void* p : arrays)
-    if (p) SVO_CUDA_TRY(cudaFreeAsync(p, st));
+  if (d.block) {
+    SVO_CUDA_TRY(cudaFreeAsync(d.block, st));
+    d.block = nullptr;
+  } else {
+    void* arrays[6] = {d.top, d.nodes, d.voxels, d.vbits, d.colors, d.datas};
+    for (void* p : arrays)
+      if (p) SVO_CUDA_TRY(cudaFreeAsync(p, st));
+  }
   d.top = d.nodes = nullptr;
   d.voxels = d.vbits = d.colors = d.datas = nullptr;
-  d.top_keys.clear();
-  for (auto& c : d.top_count) c = 0;
+  for (auto& c : d.top_count) c = 0;  // top_keys describe the host mirror, which stays
   d.node_cap = d.brick_cap = d.color_cap = d.data_cap = 0;
   d.valid = false;
   d.ordered = false;
-  // the host mirror and the dirty flags stay: uploading the scene again copies the mirror, after
-  // rebuilding what changed meanwhile
+  // the host mirror, the blob and the dirty flags stay: uploading the scene again copies the blob if
+  // nothing changed meanwhile, else rebuilds what changed and refills the blob
   return SVO_OK;
 }
 }  // namespace svo
@@ -956,6 +1066,7 @@ void svo_scene_destroy(svo_scene* sc) {
   if (!sc) return;
   destroy_pipeline(sc->dev);
   free_device(sc->dev);
+  free_blob(sc->dev);
   destroy_queues(sc->dev);
   delete sc;
 }

@@ -83,6 +83,16 @@ struct DeviceImage {
   bool valid = false;
   bool ordered = false;    // image arrays from the stream-ordered pool (a server's residency)
   bool mirror_ok = false;  // host_nodes / host_vbits / the top table match the tree but for dirty elements
+  // A server's resident image is one block of the stream-ordered pool (`block`, the arrays above point
+  // into it), copied from a pinned host image laid out like it (`blob`).  While the tree is unchanged
+  // the blob stays valid across evictions, so uploading the scene again is one allocation and
+  // asynchronous copies, with no host work.
+  void* block = nullptr;
+  uint8_t* blob = nullptr;
+  uint64_t blob_bytes = 0;
+  uint32_t blob_top_count[kMaxStageDepth + 1] = {};
+  bool blob_ok = false;
+  cudaEvent_t blob_done = nullptr;  // recorded after the last copy out of the blob
   // host mirror of the node records and voxel bits (source of in-place syncs)
   std::vector<DevNode> host_nodes;
   std::vector<uint32_t> host_vbits;

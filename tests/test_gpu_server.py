@@ -146,3 +146,59 @@ def test_budget_pressure_evicts_and_trims_with_the_same_results():
         assert srv.stats()["resident_bytes"] <= budget
     finally:
         srv.close()
+
+
+def test_evicted_scenes_upload_again_from_the_pinned_image_and_see_edits():
+    """A budget that holds one of two scenes: each request on the other scene evicts the resident one.  An
+    unchanged scene comes back from its pinned host image; a scene edited (unsynced) and then evicted, or
+    edited and synced in place while resident and then evicted, comes back with the edit.  Every result
+    equals the plain cast of a twin scene."""
+    sc, twin = scenes(), scenes()
+    image = []
+    for t in sc[:2]:
+        t.upload()
+        image.append(t.stats()["device_bytes"])
+    for t in sc + twin:
+        t.release_device()
+    # one scene always fits, two never do, and nothing is trimmed after a launch (the test edits and
+    # syncs a resident scene while the server is idle)
+    srv = svo.Server(budget_bytes=sum(image) - 1, max_batch_requests=1, max_inflight=1)
+    try:
+        for t in sc:
+            srv.add_scene(t)
+        rng = np.random.default_rng(11)
+        base = requests(sc, rng, 6)
+        a = next(r for r in base if r[0] == 0)
+        b = next(r for r in base if r[0] == 1)
+
+        def serve(r):
+            out = out_arrays(r[4], r[5])
+            srv.wait(srv.submit(*r, out=out), 60.0)
+            return out
+
+        def edit(j, k):
+            S = sc[j].size
+            pos, size = (S // 2, S // 4, S // 2 - 16 * k), 16
+            for t in (sc[j], twin[j]):
+                t.insert_at_lod(pos, size, albedo=0x11223344 + k, user=900 + k)
+
+        first = serve(a)
+        same(first, expected(twin, a))
+        for _ in range(3):  # unchanged: evicted and uploaded again
+            same(serve(b), expected(twin, b))
+            same(serve(a), first)
+        edit(0, 0)  # edited while resident, not synced; the next request evicts it
+        same(serve(b), expected(twin, b))
+        after = serve(a)
+        same(after, expected(twin, a))
+        assert not np.array_equal(after["albedo"], first["albedo"])
+        edit(0, 1)  # edited and synced in place while resident
+        sc[0].sync()
+        synced = serve(a)
+        same(synced, expected(twin, a))
+        same(serve(b), expected(twin, b))
+        same(serve(a), synced)  # uploaded again after the in-place sync: the pinned image was made again
+        st = srv.stats()
+        assert st["evictions"] >= 8 and st["uploads"] >= 10
+    finally:
+        srv.close()
