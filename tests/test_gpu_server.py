@@ -9,13 +9,20 @@ pytestmark = pytest.mark.gpu
 FIELDS = ("status", "entry_kind", "node_key", "voxel_index", "albedo", "user", "px", "py", "pz", "nx", "ny", "nz")
 
 
+SCENES = [(0, 64, 4), (3, 128, 8), (1, 64, 2)]
+
+
+def scene_ops(j):
+    kind, size, dim = SCENES[j]
+    return svo.gen_scene(kind, size, dim, seed=500 + j, occupancy=0.1, spheres=3, octaves=2, base_freq=1.0 / 16,
+                         height_lo=2.0, height_hi=size * 0.35)
+
+
 def scenes():
     out = []
-    for j, (kind, size, dim) in enumerate([(0, 64, 4), (3, 128, 8), (1, 64, 2)]):
-        ops = svo.gen_scene(kind, size, dim, seed=500 + j, occupancy=0.1, spheres=3, octaves=2, base_freq=1.0 / 16,
-                            height_lo=2.0, height_hi=size * 0.35)
+    for j, (_, size, dim) in enumerate(SCENES):
         t = svo.Octree(size, dim)
-        t.apply_ops(ops)
+        t.apply_ops(scene_ops(j))
         out.append(t)
     return out
 
@@ -202,3 +209,37 @@ def test_evicted_scenes_upload_again_from_the_pinned_image_and_see_edits():
         assert st["evictions"] >= 8 and st["uploads"] >= 10
     finally:
         srv.close()
+
+
+def test_served_results_equal_the_oracle(oracle_mod):
+    """Each request's rays are made on the device by the server; its results equal the oracle's cast of
+    the rays that the oracle's own camera generator makes for the same request."""
+    sc = scenes()
+    trees = []
+    for j, (_, size, dim) in enumerate(SCENES):
+        o = oracle_mod.Tree(size, dim)
+        o.apply_ops(scene_ops(j))
+        trees.append(o)
+    reqs = requests(sc, np.random.default_rng(5), 12)
+    srv = svo.Server(max_batch_requests=4, max_inflight=2)
+    try:
+        for t in sc:
+            srv.add_scene(t)
+        outs = [out_arrays(r[4], r[5]) for r in reqs]
+        rids = [srv.submit(*r, out=o) for r, o in zip(reqs, outs)]
+        for rid in rids:
+            srv.wait(rid, 60.0)
+    finally:
+        srv.close()
+    for r, got in zip(reqs, outs):
+        j, eye, target, fov, w, h = r
+        o, d = oracle_mod.gen_camera_rays(eye, target, fov, w, h)
+        ref = trees[j].cast(o, d)
+        for k in FIELDS:
+            a, b = got[k], np.asarray(ref[k])
+            if a.dtype.kind == "f":
+                same = (a == b) | (np.isnan(a) & np.isnan(b))
+                with np.errstate(invalid="ignore"):
+                    assert np.all(same | (np.abs(a.astype(np.float64) - b) <= 1e-4)), k
+            else:
+                assert np.array_equal(a.astype(np.uint32), b.astype(np.uint32)), k
