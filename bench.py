@@ -557,8 +557,15 @@ def run_single(args, w, workload):
         t0 = time.perf_counter()
         ref = tree.cast(origins, dirs, threads=threads)
         cpu_s = time.perf_counter() - t0
+        # one core: every 64th ray (the same rays, so it stays a bounded sample of this batch)
+        o1, d1 = np.ascontiguousarray(origins[::64]), np.ascontiguousarray(dirs[::64])
+        t0 = time.perf_counter()
+        tree.cast(o1, d1, threads=1)
+        one_s = time.perf_counter() - t0
         cpu = {"value": round(n / cpu_s / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
-               "sample": "the whole %d-ray batch, once (%.1fs on %d threads)" % (n, cpu_s, threads)}
+               "sample": "the whole %d-ray batch, once (%.1fs on %d threads)" % (n, cpu_s, threads),
+               "single_core": {"value": round(len(o1) / one_s / 1e6, 4), "unit": "Mrays/s",
+                               "sample": "every 64th ray of the batch (%d rays, %.1fs on 1 thread)" % (len(o1), one_s)}}
         parity = merge_parity([compare_hits(got, ref, label) for label, got in checks])
         del ref
     checks.clear()
