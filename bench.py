@@ -28,6 +28,7 @@ workload, with the scene and rays made by the oracle's own generators: it
 loads no product code.
 """
 import argparse
+import gc
 import json
 import os
 import subprocess
@@ -1065,6 +1066,17 @@ def run_served(args, w):
         svo.HIT_FIELDS[f]) for f in full_fields} for k in full_ids}
 
     def serve(srv, paced):
+        # the Python loop below drives the native server: a collection of the interpreter's heap in the
+        # middle of it (the process holds the earlier workloads' objects) would stall submissions, so the
+        # heap is collected before the run and the collector is off during it
+        gc.collect()
+        gc.disable()
+        try:
+            return serve_run(srv, paced)
+        finally:
+            gc.enable()
+
+    def serve_run(srv, paced):
         for t in scenes:  # every run starts with no scene resident
             t.release_device()
         ids = [srv.add_scene(t) for t in scenes]

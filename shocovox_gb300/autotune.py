@@ -70,10 +70,17 @@ def tune(ws, items, gpu_name, time_fn, use_cache=True):
     b, c, p, sh, so, _, _ = (int(v) for v in min(table, key=table.get).split("x"))
     for st in STAGING:
         table["%dx%dx%dx%dx%dx%dx0" % (b, c, p, sh, so, st)] = time_fn(_lib.LaunchConfig(b, c, p, sh, so, st, 0))
-    if so == 1:  # the sorted cast: its lane-refill threshold, at the best staging depth
+    if so == 1:
+        # the sorted cast: its lane-refill threshold at the best staging depth, for every block size (each
+        # with its best rays per claim): the refilling kernel's occupancy is not the plain kernel's, so the
+        # best block without refill need not be the best with it
         st = int(min((k for k in table if k.startswith("%dx%dx%dx%dx%dx" % (b, c, p, sh, so))), key=table.get).split("x")[5])
-        for rf in REFILL:
-            table["%dx%dx%dx%dx%dx%dx%d" % (b, c, p, sh, so, st, rf)] = time_fn(_lib.LaunchConfig(b, c, p, sh, so, st, rf))
+        for bb in BLOCKS:
+            cc = int(min((k for k in table if k.startswith("%dx" % bb) and k.endswith("x%dx%dx%dx0x0" % (p, sh, so))),
+                         key=table.get).split("x")[1])
+            for rf in REFILL:
+                table["%dx%dx%dx%dx%dx%dx%d" % (bb, cc, p, sh, so, st, rf)] = time_fn(
+                    _lib.LaunchConfig(bb, cc, p, sh, so, st, rf))
     best = min(table, key=table.get)
     b, c, p, sh, so, st, rf = (int(v) for v in best.split("x"))
     entry = {"config": [b, c, p, sh, so, st, rf], "ms": table[best], "sweep_ms": table,

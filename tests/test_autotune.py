@@ -49,13 +49,15 @@ def test_sweep_covers_the_knobs_of_the_batch(rows, want_shapes, want_sorts):
     assert {k[4] for k in seen} == want_sorts
     assert {k[0] for k in seen} == set(autotune.BLOCKS) and {k[1] for k in seen} == set(autotune.CHUNKS)
     first = len(autotune.BLOCKS) * len(autotune.CHUNKS) * len(want_shapes) * len(want_sorts)
-    refills = len(autotune.REFILL) if best[4] == 1 else 0  # the refill stage only for a sorted best
+    # the refill stage only for a sorted best, at every block size
+    refills = len(autotune.BLOCKS) * len(autotune.REFILL) if best[4] == 1 else 0
     assert len(seen) == len(set(seen)) == first + len(autotune.STAGING) + refills
     assert all(k[5] == 0 and k[6] == 0 for k in seen[:first])  # the first stage: nothing staged, no refill
     stage = seen[first:first + len(autotune.STAGING)]
     assert [k[:5] for k in stage] == [best] * len(autotune.STAGING)  # then the depths on the best
     assert {k[5] for k in stage} == set(autotune.STAGING) and all(k[6] == 0 for k in stage)
     assert {k[6] for k in seen[first + len(autotune.STAGING):]} == (set(autotune.REFILL) if refills else set())
+    assert {k[0] for k in seen[first + len(autotune.STAGING):]} == (set(autotune.BLOCKS) if refills else set())
     assert (cfg.block, cfg.rays_per_chunk, cfg.blocks_per_sm, cfg.block_shape, cfg.sort_key) == best
     assert cfg.staging_depth == 0 and cfg.refill_below == 0
     assert info["cached"] is False and info["config"] == list(best) + [0, 0]
