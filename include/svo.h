@@ -427,7 +427,9 @@ svo_status svo_set_cast_mode(int32_t mode);
  * the host buffers in place for batches with a row layout (svo_cast_host_rows, row_length >= 16)
  * when the device accesses host memory through the CPU's page tables (Grace systems), and stages
  * copies otherwise; 1 always stages copies (chunks over three streams); 2 always accesses host
- * memory directly (an error where the device cannot). */
+ * memory directly (an error where the device cannot); 3 as 2, with each warp writing its own 16 x 2
+ * ray block (pieces of 64 and 16 bytes a row) instead of two blocks' rows of 32 rays (pieces of 128
+ * and 32 bytes), for comparison. */
 svo_status svo_set_host_transfer(int32_t mode);
 /* Staging depth of the plain casts launched afterwards (svo_cast, svo_cast_rows and the host-buffer
  * casts; process-wide): each block first copies the scene's Internal nodes of depth < depth (the

@@ -308,6 +308,98 @@ __global__ void __launch_bounds__(128, 7)
   }
 }
 
+// Host-buffer cast that reads its rays from and writes its hits to host memory in place (over the CPU
+// link).  Stores to host memory cost by the piece, and a warp's 16 x 2 ray block gives pieces of 64
+// bytes (4-byte fields) and 16 bytes (1-byte fields) per row.  Here a warp claims two neighbouring
+// 16 x 2 blocks (a 32 x 2 block of the image), casts them one after the other -- so that it keeps the
+// lock-step of 16 x 2 blocks -- keeps their records in shared memory, and then writes each field row
+// by row: 32 neighbouring rays, pieces of 128 and 32 bytes.  The records are those of queue_kernel.
+struct PairStage {  // one warp's two blocks, a field at a time (no bank conflicts)
+  uint32_t node[64], voxel[64], pix[64], albedo[64], user[64];
+  float px[64], py[64], pz[64], nx[64], ny[64], nz[64];
+  uint32_t small[64];  // status | octant << 8 | entry kind << 16
+};
+
+__global__ void __launch_bounds__(128, 7)
+    pair_rows_kernel(SceneView s, RaysView rays, HitsView out, uint64_t n, ClaimOrder order,
+                     unsigned long long* __restrict__ counter) {
+  __shared__ SharedLuts L;
+  __shared__ PairStage stage[4];
+  fill_shared_luts(L);
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31u;
+  PairStage& ps = stage[threadIdx.x >> 5];
+  for (;;) {
+    unsigned long long c = 0;
+    if (lane == 0) c = atomicAdd(counter, 2ull);
+    c = __shfl_sync(0xFFFFFFFFu, c, 0);
+    if (c >= order.claims) break;
+    for (uint32_t half = 0; half < 2; ++half) {
+      const uint64_t cc = c + half;
+      const uint64_t j = cc < order.claims ? claimed_ray(order, cc, lane, n) : n;
+      HitRecord h;
+      miss_record(h);
+      if (j < n) {
+        const float ox = __ldg(rays.ox + j), oy = __ldg(rays.oy + j), oz = __ldg(rays.oz + j);
+        const float dx = __ldg(rays.dx + j), dy = __ldg(rays.dy + j), dz = __ldg(rays.dz + j);
+        const bool fast = !s.literal && !isnan(dx) && !isnan(dy) && !isnan(dz);
+        float px = 0.0f, py = 0.0f, pz = 0.0f;
+        uint32_t target = 0;
+        if (!fast || fast_entry(s, ox, oy, oz, dx, dy, dz, px, py, pz, target))
+          cast_entered<false>(s, L, ox, oy, oz, dx, dy, dz, fast, px, py, pz, target, h);
+      }
+      // write_hit's record, kept for the rows below
+      uint32_t kind, albedo, user;
+      resolve_entry(s, h, kind, albedo, user);
+      if (h.status != 1) {
+        h.octant = h.node = h.pix = 0;
+        h.voxel = 0xFFFFFFFFu;
+        h.px = h.py = h.pz = h.nx = h.ny = h.nz = 0.0f;
+        kind = albedo = user = 0;
+      }
+      const uint32_t k = half * 32u + lane;
+      ps.node[k] = h.node;
+      ps.voxel[k] = h.voxel;
+      ps.pix[k] = h.pix;
+      ps.albedo[k] = albedo;
+      ps.user[k] = user;
+      ps.px[k] = h.px;
+      ps.py[k] = h.py;
+      ps.pz[k] = h.pz;
+      ps.nx[k] = h.nx;
+      ps.ny[k] = h.ny;
+      ps.nz[k] = h.nz;
+      ps.small[k] = (h.status & 0xFFu) | ((h.octant & 0xFFu) << 8) | ((kind & 0xFFu) << 16);
+    }
+    __syncwarp();
+    // row r of the 32 x 2 block: lanes 0-15 the first block's columns, lanes 16-31 the second's
+    for (uint32_t r = 0; r < 2; ++r) {
+      const uint32_t half = lane >> 4, bl = (r << 4) | (lane & 15u);
+      const uint64_t cc = c + half;
+      const uint64_t j = cc < order.claims ? claimed_ray(order, cc, bl, n) : n;
+      if (j < n) {
+        const uint32_t k = half * 32u + bl;
+        const uint32_t sm = ps.small[k];
+        if (out.status) out.status[j] = (uint8_t)sm;
+        if (out.octant) out.octant[j] = (uint8_t)(sm >> 8);
+        if (out.kind) out.kind[j] = (uint8_t)(sm >> 16);
+        if (out.node) out.node[j] = ps.node[k];
+        if (out.voxel) out.voxel[j] = ps.voxel[k];
+        if (out.pix) out.pix[j] = ps.pix[k];
+        if (out.albedo) out.albedo[j] = ps.albedo[k];
+        if (out.user) out.user[j] = ps.user[k];
+        if (out.px) out.px[j] = ps.px[k];
+        if (out.py) out.py[j] = ps.py[k];
+        if (out.pz) out.pz[j] = ps.pz[k];
+        if (out.nx) out.nx[j] = ps.nx[k];
+        if (out.ny) out.ny[j] = ps.ny[k];
+        if (out.nz) out.nz[j] = ps.nz[k];
+      }
+    }
+    __syncwarp();
+  }
+}
+
 constexpr uint64_t kQueueMinRays = 1u << 15;  // below this the one-thread-per-ray grid is as fast
 
 void destroy_queues(DeviceImage& d) {
@@ -357,6 +449,7 @@ int g_cast_mode = 0;
 int g_host_transfer = 0;  // svo_set_host_transfer: 0 auto, 1 staged copies, 2 direct access
 int g_stage_depth = 0;    // svo_set_staging_depth: top levels the plain casts stage in shared memory
 int g_refill_below = 0;   // svo_set_refill: a warp parks and refills below this many rays in flight
+int g_pair_rows = 1;      // host buffers read and written in place: 32 x 2 blocks written row by row
 
 // ------------------------------------------------------------------ device image
 uint64_t device_image_bytes(const svo_scene* sc) {
@@ -833,7 +926,9 @@ svo_status launch_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const sv
       SVO_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st));
       const ClaimOrder order = claim_order(n, row, in_place ? 4 : 3);
       const uint32_t stage_n = g_cast_mode == 1 ? 0u : staged_records(sc, (uint32_t)g_stage_depth);
-      if (g_refill_below > 0) {
+      if (in_place && !count && stage_n == 0 && g_refill_below == 0 && g_pair_rows) {
+        pair_rows_kernel<<<(unsigned)grid, block, 0, st>>>(v, rv, hv, n, order, ctr);
+      } else if (g_refill_below > 0) {
         const size_t smem = (size_t)stage_n * sizeof(DevNode);
         auto kern = stage_n ? (count ? refill_kernel<true, true> : refill_kernel<false, true>)
                             : (count ? refill_kernel<true> : refill_kernel<false>);
@@ -1169,8 +1264,9 @@ svo_status svo_cast_host(svo_scene* sc, const svo_rays* rays, uint64_t n, const 
 }
 
 svo_status svo_set_host_transfer(int32_t mode) {
-  if (mode < 0 || mode > 2) return fail(SVO_ERR_ARGUMENT, "svo_set_host_transfer: mode must be 0, 1 or 2");
-  g_host_transfer = mode;
+  if (mode < 0 || mode > 3) return fail(SVO_ERR_ARGUMENT, "svo_set_host_transfer: mode must be 0, 1, 2 or 3");
+  g_host_transfer = mode == 3 ? 2 : mode;
+  g_pair_rows = mode == 3 ? 0 : 1;
   return SVO_OK;
 }
 

@@ -318,14 +318,18 @@ def test_row_layout_casts_equal_plain_casts(oracle_mod):
     # (with and without counters: the instrumented cast is a kernel of its own; mode 2 reads host
     # memory in place even without a row layout, where the device can)
     no_counters = [k for k in svo.HIT_FIELDS if k not in COUNTERS + ["run_visits"]]
+    direct = False
     if svo.lib().svo_set_host_transfer(2) == 0:
         try:
+            direct = True
             same(p.cast_host(origins, dirs), plain, "host in place, plain order")
             same(p.cast_host(origins, dirs, fields=no_counters, row_length=W), {k: plain[k] for k in no_counters},
                  "host in place, rows")
         finally:
             svo.lib().svo_set_host_transfer(0)
-    for mode in (0, 1):
+    # 0: rows in place as 32 x 2 blocks written row by row (where the device reads host memory), 1: staged,
+    # 3: rows in place, each warp writing its own 16 x 2 block
+    for mode in (0, 1) + ((3,) if direct else ()):
         assert svo.lib().svo_set_host_transfer(mode) == 0
         try:
             same(p.cast_host(origins, dirs, row_length=W), plain, "host rows, transfer mode %d" % mode)
