@@ -18,7 +18,7 @@ cameras at 1920x1080 and 70 deg FOV at seeded positions above the terrain:
           normal within 1e-4 voxel units.  A mismatch makes the run exit 1.
 
 The default run also measures, in sub-objects of its one JSON line
-("north_star"), the plain cast against the batched and served forms on the
+("comparisons"), the plain cast against the batched and served forms on the
 incoherent-ray, multi-scene and served workloads, each over repeated timings
 with its own parity check and clock record.
 
@@ -69,7 +69,7 @@ COUNTERS = ("node_visits", "child_reads", "voxel_reads", "run_visits")
 OUT_BYTES = {"status": 1, "entry_kind": 1, "albedo": 4, "user": 4, "px": 4, "py": 4, "pz": 4, "nx": 4, "ny": 4,
              "nz": 4}
 RAY_KEYS = ("ox", "oy", "oz", "dx", "dy", "dz")
-REPEATS = 5  # timed repeats of each spec variant (median and spread are reported)
+REPEATS = 5  # timed repeats of each compared variant (median and spread are reported)
 
 # ---- parity against the oracle --------------------------------------------------------------------
 TOL = 1e-4  # voxel units: impact point and normal
@@ -619,8 +619,8 @@ def run_single(args, w, workload):
     return rec, pg
 
 
-# ---- north star (a): incoherent rays, plain cast vs batched forms ---------------------------------
-def north_star_incoherent(args):
+# ---- comparison (a): incoherent rays, plain cast vs batched forms ---------------------------------
+def compare_incoherent(args):
     """incoherent1024: plain svo_cast against the autotuned persistent batched cast in index order and
     with the ray sort, timed over interleaved repeats, every variant's hits checked against the oracle."""
     import torch
@@ -694,7 +694,7 @@ def north_star_incoherent(args):
             "parity": parity, "clocks": clk}
 
 
-# ---- north star (b): many scenes in one persistent launch ------------------------------------------
+# ---- comparison (b): many scenes in one persistent launch ------------------------------------------
 def multiscene_specs(w):
     """64 scenes: size from {64..512}^3, brick dim from {2,4,8}, occupancy 2-20%, noise + spheres,
     a log-uniform 1K-1M ray batch each (half camera rays, half random directions)."""
@@ -965,7 +965,7 @@ def dev_out_clear(d):
         v.zero_()
 
 
-# ---- north star (c): served requests --------------------------------------------------------------
+# ---- comparison (c): served requests --------------------------------------------------------------
 SERVE_STRIDE = 1024  # every request: its pixels first, first + 1024, ... are checked against the oracle
 SERVE_FULL_EVERY = 500  # every 500th request also returns every hit field and is checked in full
 SERVE_FIELDS = ("status", "albedo")  # what every request returns to host memory
@@ -1579,7 +1579,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="terrain512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle checks (and the CPU baseline)")
-    ap.add_argument("--no-north-star", action="store_true",
+    ap.add_argument("--no-comparisons", action="store_true",
                     help="skip the incoherent1024 / multiscene64 / served16 comparisons of the default run")
     ap.add_argument("--no-variants", action="store_true", help="skip the persistent-kernel autotune sweep")
     ap.add_argument("--refill", type=int, default=0,
@@ -1607,16 +1607,16 @@ def main():
     else:
         rec, pg = run_single(args, w, args.workload)
         _, _, world = dist_env()
-        if args.workload == "terrain512" and world == 1 and not args.no_north_star:
+        if args.workload == "terrain512" and world == 1 and not args.no_comparisons:
             ns = {}
-            for name, fn in (("incoherent1024", lambda: north_star_incoherent(args)),
+            for name, fn in (("incoherent1024", lambda: compare_incoherent(args)),
                              ("multiscene64", lambda: run_multiscene(args, WORKLOADS["multiscene64"])),
                              ("served16", lambda: run_served(args, WORKLOADS["served16"]))):
                 try:
                     ns[name] = fn()
                 except Exception as e:  # recorded in the line (and fails the run), the other parts still report
                     ns[name] = {"error": "%s: %s" % (type(e).__name__, e)}
-            rec["north_star"] = ns
+            rec["comparisons"] = ns
     rank, _, _ = dist_env()
     if rank == 0:
         print(json.dumps(rec))

@@ -1,9 +1,9 @@
 """ctypes binding of the CPU oracle library (TEST INFRASTRUCTURE ONLY).
 
 The oracle is a plain CPU restatement of shocovox-rs v0.11.1's octree and
-`Octree::get_by_ray` (see svo_oracle.cpp).  It is the checker for the GB300
-product library and the timed CPU baseline; nothing in the product path
-imports this module.
+`Octree::get_by_ray` (see svo_oracle.cpp).  The tests compare the GB300
+product library against it, and the bench times it as the CPU baseline;
+nothing in the product path imports this module.
 """
 import ctypes
 import os

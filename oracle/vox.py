@@ -8,8 +8,8 @@ appearance, a voxel's colour index one less than the stored one (saturating at
 0) selecting entry i of the RGBA chunk, attribute dictionaries where the last
 repeated key wins.  It yields the octree size and the insert sequence; the
 oracle's Tree applies them.  Where the reference panics this raises VoxPanic;
-malformed bytes raise VoxFormatError.  It is the checker for the product's
-importer and is not imported by the product.
+malformed bytes raise VoxFormatError.  The tests compare the product's importer
+against it; the product does not import it.
 """
 import math
 import struct

@@ -115,6 +115,6 @@ def test_parity_helpers():
     assert r["mismatches"] == 2 and set(r["first_mismatch"]) == {"px", "node_key"}
     m = bench.merge_parity([bench.compare_hits(same, ref, "a"), r])
     assert m["mismatches"] == 2 and m["rays_checked"] == 6
-    assert bench.parity_failed({"north_star": {"x": {"parity": m}}})
+    assert bench.parity_failed({"comparisons": {"x": {"parity": m}}})
     assert not bench.parity_failed({"parity": bench.merge_parity([bench.compare_hits(same, ref)])})
-    assert bench.parity_failed({"north_star": {"served16": {"error": "RuntimeError: x"}}})
+    assert bench.parity_failed({"comparisons": {"served16": {"error": "RuntimeError: x"}}})
