@@ -376,10 +376,13 @@ typedef struct {
 
 /* Starts the server and its worker thread on the current device. */
 svo_status svo_server_create(const svo_server_config* cfg, svo_server** out);
-/* Stops the worker after the requests in flight complete and releases the server's device memory. */
+/* Stops the worker after the requests submitted so far complete (or fail: a launch that fails on
+ * the device fails its requests) and releases the server's device memory. */
 void svo_server_destroy(svo_server* server);
 /* Registers a scene (not owned; the caller keeps it alive and leaves it untouched while registered).
- * The server uploads and evicts its device image under the budget. */
+ * The server uploads and evicts its device image under the budget; a launch waits for the uploads of
+ * its scenes made on other launches' streams.  A device image the caller uploaded must be complete
+ * (its stream synchronised) before the scene is registered. */
 svo_status svo_server_add_scene(svo_server* server, svo_scene* scene, uint32_t* scene_id);
 /* Queues a request; returns at once with its id. */
 svo_status svo_server_submit(svo_server* server, const svo_request* request, uint64_t* request_id);

@@ -1096,7 +1096,12 @@ extern "C" {
 namespace svo {
 svo_status upload_ordered(svo_scene* sc, cudaStream_t st) {
   TraceRange range("svo_scene_upload (stream-ordered)");
-  return full_upload(sc, st, true);
+  const svo_status rc = full_upload(sc, st, true);
+  if (rc != SVO_OK) return rc;
+  DeviceImage& d = sc->dev;
+  if (!d.ready) SVO_CUDA_TRY(cudaEventCreateWithFlags(&d.ready, cudaEventDisableTiming));
+  SVO_CUDA_TRY(cudaEventRecord(d.ready, st));
+  return SVO_OK;
 }
 
 svo_status evict_ordered(svo_scene* sc, cudaStream_t st) {
@@ -1162,6 +1167,7 @@ void svo_scene_destroy(svo_scene* sc) {
   destroy_pipeline(sc->dev);
   free_device(sc->dev);
   free_blob(sc->dev);
+  if (sc->dev.ready) cudaEventDestroy(sc->dev.ready);
   destroy_queues(sc->dev);
   delete sc;
 }

@@ -93,6 +93,9 @@ struct DeviceImage {
   uint32_t blob_top_count[kMaxStageDepth + 1] = {};
   bool blob_ok = false;
   cudaEvent_t blob_done = nullptr;  // recorded after the last copy out of the blob
+  // recorded on the upload's stream after a server's upload of the image: a launch on another stream
+  // waits for it before it reads the image
+  cudaEvent_t ready = nullptr;
   // host mirror of the node records and voxel bits (source of in-place syncs)
   std::vector<DevNode> host_nodes;
   std::vector<uint32_t> host_vbits;
@@ -125,7 +128,8 @@ svo_status fail(svo_status code, const std::string& msg);
 SceneView scene_view(const svo_scene* s);
 // A server's residency: the image allocated from the stream-ordered pool on `st` (unless the caller's
 // allocator is installed), and given back the same way, so that evicting one scene and uploading
-// another does not wait for the whole device.  The evicted scene must have no cast in flight.
+// another does not wait for the whole device.  The evicted scene must have no cast in flight.  The
+// upload records DeviceImage::ready on `st`: a cast on another stream waits for it.
 svo_status upload_ordered(svo_scene* s, cudaStream_t st);
 svo_status evict_ordered(svo_scene* s, cudaStream_t st);
 // records of the top table that a cast with staging depth `depth` copies (0 when the scene has none)

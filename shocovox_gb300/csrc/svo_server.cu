@@ -205,6 +205,11 @@ svo_status launch(svo_server* sv, LaunchSlot& ls, size_t n_scenes, LaunchCounts&
   }
   svo_status rc = make_resident(sv, ls.scenes, n_scenes, ls.st, cnt);
   if (rc != SVO_OK) return rc;
+  // a scene uploaded for another slot may still be in its copies on that slot's stream
+  for (uint32_t id : ls.scenes) {
+    const cudaEvent_t ready = sv->scenes[id].scene->dev.ready;
+    if (ready) SRV_CUDA(cudaStreamWaitEvent(ls.st, ready, 0));
+  }
   std::vector<svo_batch_item> items(ls.reqs.size());
   size_t o = 0;
   for (size_t i = 0; i < ls.reqs.size(); ++i) {
@@ -257,13 +262,23 @@ void worker_main(svo_server* sv) {
     // retire finished launches
     cudaStream_t idle_stream = nullptr;
     for (LaunchSlot& ls : sv->slots) {
-      if (!ls.busy || cudaEventQuery(ls.done) != cudaSuccess) continue;
+      if (!ls.busy) continue;
+      const cudaError_t e = cudaEventQuery(ls.done);
+      if (e == cudaErrorNotReady) continue;
       idle_stream = ls.st;
       TraceRange range("svo_server retire");
       const double t = now_s();
+      if (e != cudaSuccess) {  // the launch failed on the device: its requests fail, none waits forever
+        set_error(std::string("svo_server: launch failed: ") + cudaGetErrorString(e));
+        idle_stream = nullptr;
+      }
       for (Request* q : ls.reqs) {
         q->t_done = t;
         q->done = true;
+        if (e != cudaSuccess) {
+          q->status = SVO_ERR_CUDA;
+          continue;
+        }
         sv->stats.requests_done++;
         sv->stats.rays_done += q->n;
       }
