@@ -380,3 +380,29 @@ def test_work_queue_with_rays_missing_the_root(oracle_mod):
                 assert_same_hits(g, want, counters=with_counters, label="queue mode %d" % mode)
         finally:
             svo.lib().svo_set_cast_mode(0)
+
+
+def test_in_place_host_rows_with_special_rays(oracle_mod):
+    """svo_cast_host_rows read and written in place (two 16 x 2 blocks per warp, each field written row by
+    row): camera rays with random rays mixed in (origins outside and inside the octree, axis-aligned and
+    NaN / infinite / zero / subnormal directions, which take the literal form) equal the oracle's cast,
+    for row lengths with partial blocks, odd numbers of claims and a tail of 32-ray claims."""
+    ops = svo.gen_scene(3, 128, 4, seed=97, occupancy=0.1, spheres=5, octaves=2, base_freq=1.0 / 16)
+    o, p = both(oracle_mod, 128, 4, ops)
+    W, H = 250, 163  # 40,750 rays: above the work-queue threshold
+    origins, dirs = svo.gen_camera_rays([190.0, 140.0, 210.0], [64.0, 50.0, 64.0], 60.0, W, H)
+    rng = np.random.default_rng(5)
+    mixed = rng.choice(len(origins), 2000, replace=False)
+    ro, rd = random_rays(rng, 128, 2000)
+    origins, dirs = origins.copy(), dirs.copy()
+    origins[mixed], dirs[mixed] = ro, rd
+    ref = o.cast(origins, dirs, threads=8)
+    fields = [k for k in svo.HIT_FIELDS if k not in COUNTERS + ["run_visits"]]
+    if svo.lib().svo_set_host_transfer(2) != 0:
+        pytest.skip("this device does not read host memory in place")
+    try:
+        for row in (W, 16, 17, 31, 33, 1000, 40_000):
+            got = p.cast_host(origins, dirs, fields=fields, row_length=row)
+            assert_same_hits(got, ref, label="in place, rows of %d" % row)
+    finally:
+        svo.lib().svo_set_host_transfer(0)
