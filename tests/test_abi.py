@@ -97,3 +97,23 @@ def test_struct_layouts_match_bindings(tmp_path):
         cls = pairs[name]
         for f in fields:
             assert int(got["%s.%s" % (name, f)]) == getattr(cls, f).offset, (name, f)
+
+
+def test_process_wide_knobs_check_their_ranges():
+    """The setters of the cast knobs accept their documented ranges and refuse the rest (no GPU needed:
+    they only set process-wide values)."""
+    lib = svo.lib()
+    try:
+        for mode in range(4):  # host transfer: auto, staged, in place, in place one block per warp
+            assert lib.svo_set_host_transfer(mode) == 0
+        assert lib.svo_set_host_transfer(4) == 6 and lib.svo_set_host_transfer(-1) == 6
+        for t in (0, 1, 24, 32):
+            assert lib.svo_set_refill(t) == 0
+        assert lib.svo_set_refill(33) == 6 and lib.svo_set_refill(-1) == 6
+        for k in range(5):
+            assert lib.svo_set_staging_depth(k) == 0
+        assert lib.svo_set_staging_depth(5) == 6
+    finally:
+        lib.svo_set_host_transfer(0)
+        lib.svo_set_refill(0)
+        lib.svo_set_staging_depth(0)
