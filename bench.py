@@ -580,7 +580,8 @@ def run_single(args, w, workload):
         l2 = {"bytes_per_launch": prof["l2_bytes_per_launch"],
               "gbs": round(prof["l2_bytes_per_launch"] / (ms_step / 1e3) / 1e9, 1),
               "hit_rate_pct": prof.get("l2_hit_rate_pct"), "l1_hit_rate_pct": prof.get("l1_hit_rate_pct"),
-              "frac_of_l2_peak": round(prof["l2_throughput_pct_of_peak"] / 100.0, 4),
+              "frac_of_l2_peak": (round(prof["l2_throughput_pct_of_peak"] / 100.0, 4)
+                                  if prof.get("l2_throughput_pct_of_peak") is not None else None),
               "source": "ncu capture of one launch (profiles/); gbs with this run's kernel time"}
     io_bytes = n * 24 + n * sum(OUT_BYTES.values())
     st = scene.stats()
