@@ -926,7 +926,10 @@ svo_status launch_cast(svo_scene* sc, const svo_rays* rays, uint64_t n, const sv
       SVO_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st));
       const ClaimOrder order = claim_order(n, row, in_place ? 4 : 3);
       const uint32_t stage_n = g_cast_mode == 1 ? 0u : staged_records(sc, (uint32_t)g_stage_depth);
-      if (in_place && !count && stage_n == 0 && g_refill_below == 0 && g_pair_rows) {
+      // two blocks per claim halve the units of work: only where every resident warp gets at least four
+      // of them (a small batch keeps the per-block claims, whose tail is shorter)
+      const uint64_t warps = (uint64_t)q->sm_count * (uint64_t)per_sm * (block / 32);
+      if (in_place && !count && stage_n == 0 && g_refill_below == 0 && g_pair_rows && n >= warps * 64 * 4) {
         pair_rows_kernel<<<(unsigned)grid, block, 0, st>>>(v, rv, hv, n, order, ctr);
       } else if (g_refill_below > 0) {
         const size_t smem = (size_t)stage_n * sizeof(DevNode);

@@ -389,11 +389,13 @@ def test_in_place_host_rows_with_special_rays(oracle_mod):
     for row lengths with partial blocks, odd numbers of claims and a tail of 32-ray claims."""
     ops = svo.gen_scene(3, 128, 4, seed=97, occupancy=0.1, spheres=5, octaves=2, base_freq=1.0 / 16)
     o, p = both(oracle_mod, 128, 4, ops)
-    W, H = 250, 163  # 40,750 rays: above the work-queue threshold
+    # 1,440,000 rays: enough for at least four two-block claims per resident warp (smaller batches keep
+    # the per-block claims)
+    W, H = 1600, 900
     origins, dirs = svo.gen_camera_rays([190.0, 140.0, 210.0], [64.0, 50.0, 64.0], 60.0, W, H)
     rng = np.random.default_rng(5)
-    mixed = rng.choice(len(origins), 2000, replace=False)
-    ro, rd = random_rays(rng, 128, 2000)
+    mixed = rng.choice(len(origins), 4000, replace=False)
+    ro, rd = random_rays(rng, 128, 4000)
     origins, dirs = origins.copy(), dirs.copy()
     origins[mixed], dirs[mixed] = ro, rd
     ref = o.cast(origins, dirs, threads=8)
@@ -401,7 +403,7 @@ def test_in_place_host_rows_with_special_rays(oracle_mod):
     if svo.lib().svo_set_host_transfer(2) != 0:
         pytest.skip("this device does not read host memory in place")
     try:
-        for row in (W, 16, 17, 31, 33, 1000, 40_000):
+        for row in (W, 16, 17, 31, 33, 1000, 800_000):
             got = p.cast_host(origins, dirs, fields=fields, row_length=row)
             assert_same_hits(got, ref, label="in place, rows of %d" % row)
     finally:
