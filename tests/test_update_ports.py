@@ -315,3 +315,129 @@ def test_invalid_arguments(backend):  # octree/mod.rs:173-186 and insert.rs:106-
     t = tree(backend, 4, 1)
     assert t.insert((4, 0, 0), albedo=RED) == 4   # InvalidPosition
     assert t.clear((0, 9, 0)) == 4
+
+
+# ---- the remaining cases of tests.rs: uniform parted leaves split by an insert, LOD inserts and clears at
+# unaligned positions and sizes, whole-node clears and overwrites, and two edge cases
+
+def cube(n, lo=0):
+    return [(x, y, z) for x in range(lo, n) for y in range(lo, n) for z in range(lo, n)]
+
+
+def hits_of(t, positions, value):
+    """Count of non-empty entries at `positions`, each of which must equal `value`."""
+    got = [t.get(p) for p in positions]
+    assert all(g in (E, value) for g in got), [(p, g) for p, g in zip(positions, got) if g not in (E, value)][:4]
+    return sum(g != E for g in got)
+
+
+def test_uniform_parted_brick_leaf_separated_by_insert_where_dim_is_4(backend):  # tests.rs:694-771
+    D = 4
+    t = tree(backend, 8, D)
+
+    def color(x, y, z):  # the brick's 2x2x2 cells share a colour: the leaf is downsampled losslessly
+        return ((x - x % (D // 2)) << 24) | ((y - y % (D // 2)) << 16) | ((z - z % (D // 2)) << 8) | 0xFF
+
+    for o in OFFS:
+        for x, y, z in cube(D):
+            p = (o[0] * D + x, o[1] * D + y, o[2] * D + z)
+            t.insert(p, albedo=color(x, y, z))
+            assert t.get(p) == V(color(x, y, z)), p
+    assert t.get((0, 0, 0)) == V(0x000000FF)
+    t.insert((1, 1, 1), albedo=0xFF0000FF)  # splits the uniform leaf
+    assert t.get((1, 1, 1)) == V(0xFF0000FF) and t.get((0, 0, 0)) == V(0x000000FF)
+    for o in OFFS:
+        for x, y, z in cube(D):
+            p = (o[0] * D + x, o[1] * D + y, o[2] * D + z)
+            want = V(0xFF0000FF) if p == (1, 1, 1) else V(color(x, y, z))
+            assert t.get(p) == want, p
+
+
+@pytest.mark.parametrize("size,dim,pos,lod,region,want", [
+    (8, 4, (1, 1, 1), 4, 4, 27),  # tests.rs:773-811: one brick is updated, from 1,1,1 to 3,3,3
+    (8, 1, (2, 2, 2), 3, 8, 8),   # tests.rs:813-843: the size rounds down to 2
+    (8, 1, (3, 3, 3), 3, 8, 1),   # tests.rs:845-876: a brick corner, one voxel
+    (8, 4, (1, 1, 1), 3, 8, 27),  # tests.rs:878-910
+])
+def test_insert_at_lod_unaligned(backend, size, dim, pos, lod, region, want):
+    t = tree(backend, size, dim, False)
+    t.insert_at_lod(pos, lod, albedo=RED)
+    assert t.get(pos) == V(RED)
+    assert hits_of(t, cube(region), V(RED)) == want
+
+
+def test_clear_edge_case(backend):  # tests.rs:1227-1278
+    red = 0xFF0000FF
+    t = tree(backend, 64, 16)
+    t.update((1, 0, 0), user=0xFACEFEED)
+    t.insert_at_lod((0, 0, 0), 32, albedo=red)
+    t.clear_at_lod((5, 5, 5), 8)
+    assert all(t.get(p) == E for p in cube(8, 5))
+    assert all(t.get(p) == V(red) for p in cube(5))
+    t.clear_at_lod((0, 0, 0), 32)
+    assert all(t.get(p) == E for p in cube(32))
+
+
+@pytest.mark.parametrize("dim,pos,lod,want", [
+    (1, (0, 0, 0), 2, 64 - 8),  # tests.rs:1280-1313
+    (2, (0, 0, 0), 2, 64 - 8),  # tests.rs:1316-1349
+    (1, (0, 0, 0), 3, 64 - 8),  # tests.rs:1465-1495: the size rounds down to 2
+])
+def test_clear_at_lod_in_a_size_4_block(backend, dim, pos, lod, want):
+    t = tree(backend, 8, dim)
+    t.insert_at_lod((0, 0, 0), 4, albedo=0xFFAAEEFF)
+    t.clear_at_lod(pos, lod)
+    assert hits_of(t, cube(4), V(0xFFAAEEFF)) == want
+
+
+def test_clear_at_lod_with_unaligned_position(backend):  # tests.rs:1352-1405
+    t = tree(backend, 8, 1)
+    t.insert_at_lod((0, 0, 0), 4, albedo=0xFFAAEEFF)
+    t.clear_at_lod((1, 1, 1), 2)  # clears the aligned 2-cube that holds 1,1,1
+    assert all(t.get(p) == E for p in cube(2))
+    for p in [(0, 0, 2), (0, 2, 0), (0, 2, 2), (2, 0, 0), (2, 0, 2), (2, 2, 0), (2, 2, 2)]:
+        assert t.get(p) != E, p
+    assert hits_of(t, cube(4), V(0xFFAAEEFF)) == 64 - 8
+
+
+def test_clear_at_lod_with_unaligned_position_where_dim_is_4(backend):  # tests.rs:1407-1463
+    t = tree(backend, 16, 4)
+    t.insert_at_lod((0, 0, 0), 8, albedo=0xFFAAEEFF)
+    assert all(t.get(p) == V(0xFFAAEEFF) for p in cube(8))
+    t.clear_at_lod((1, 1, 1), 4)  # one brick is updated: 1,1,1 to 3,3,3
+    assert hits_of(t, cube(8), V(0xFFAAEEFF)) == 512 - 27
+
+
+@pytest.mark.parametrize("size,set_lod,clear_lod,want_before,want_after", [
+    (8, 4, 3, 64, 64 - 27),      # tests.rs:1498-1547
+    (16, 8, 5, 512, 512 - 64),   # tests.rs:1549-1598: clears whole nodes
+])
+def test_clear_at_lod_where_dim_is_4(backend, size, set_lod, clear_lod, want_before, want_after):
+    t = tree(backend, size, 4)
+    t.insert_at_lod((0, 0, 0), set_lod, albedo=0xFFAAEEFF)
+    assert hits_of(t, cube(8), V(0xFFAAEEFF)) == want_before
+    t.clear_at_lod((0, 0, 0), clear_lod)
+    assert hits_of(t, cube(8), V(0xFFAAEEFF)) == want_after
+
+
+def test_overwrite_whole_nodes_where_dim_is_4(backend):  # tests.rs:1600-1655
+    t = tree(backend, 16, 4)
+    t.insert_at_lod((0, 0, 0), 8, albedo=RED)
+    assert hits_of(t, cube(8), V(RED)) == 512
+    t.insert_at_lod((0, 0, 0), 5, albedo=BLUE)
+    got = [t.get(p) for p in cube(8)]
+    assert E not in got
+    assert sum(g == V(RED) for g in got) == 512 - 64 and sum(g == V(BLUE) for g in got) == 64
+
+
+def test_edge_case_octree_set(backend):  # tests.rs:1657-1673
+    t = tree(backend, 8, 1)
+    for x, y, z in cube(8, 6):
+        t.insert((x, y, z), albedo=x + y + z)
+        assert t.get((x, y, z)) == V(x + y + z)
+
+
+def test_case_inserting_empty(backend):  # tests.rs:1675-1687
+    t = tree(backend, 4, 1)
+    t.insert((3, 0, 0), albedo=0)
+    assert t.get((3, 0, 0)) == E
