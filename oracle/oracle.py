@@ -111,6 +111,7 @@ def lib():
         L.orc_dda_step.argtypes = [vp, vp, vp, vp]
         L.orc_flat_projection.argtypes = [u64, u64, u64, u64]
         L.orc_flat_projection.restype = u64
+        L.orc_brick_empty_throughout.argtypes = [vp, u32, u32, u32, ctypes.c_int32, vp, u32, vp, u32]
         L.orc_stack_new.argtypes = [u32]
         L.orc_stack_new.restype = vp
         L.orc_stack_free.argtypes = [vp]
@@ -332,6 +333,18 @@ def child_bounds(cube, octant):
 
 def flat_projection(x, y, z, size):
     return lib().orc_flat_projection(x, y, z, size)
+
+
+def brick_empty_throughout(kind, pix, dim, octant, colors, datas, part=-1):
+    """BrickData::is_empty_throughout (part < 0) or is_part_empty_throughout(octant, part) of a brick of
+    kind 0 Empty, 1 Solid (pix[0]) or 2 Parted (dim^3 values) against the given palettes."""
+    p = np.ascontiguousarray(np.asarray(pix if len(pix) else [0], dtype=np.uint32))
+    c = np.ascontiguousarray(np.asarray(colors if len(colors) else [0], dtype=np.uint32))
+    d = np.ascontiguousarray(np.asarray(datas if len(datas) else [0], dtype=np.uint32))
+    rc = lib().orc_brick_empty_throughout(_ptr(p), dim, kind, octant, part, _ptr(c), len(colors), _ptr(d), len(datas))
+    if rc not in (0, 1):
+        raise OracleError(rc, "brick_empty_throughout")
+    return rc == 1
 
 
 class Stack:

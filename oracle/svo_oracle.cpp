@@ -2449,6 +2449,30 @@ void orc_dda_step(const float ray[6], float point[3], const float cube[4], float
 }
 uint64_t orc_flat_projection(uint64_t x, uint64_t y, uint64_t z, uint64_t size) { return flat_projection(x, y, z, size); }
 
+// BrickData::is_empty_throughout / is_part_empty_throughout (node.rs:75-209) on a brick of kind 0
+// (Empty), 1 (Solid: pix[0]) or 2 (Parted: dim^3 values) against the given palettes: 1 empty, 0 not,
+// ORC_ERR_REFERENCE_PANIC where the reference panics.  part < 0: the whole octant; else part is the octant of
+// the part inside it (the brick tests of src/octree/tests.rs:8-158).
+int orc_brick_empty_throughout(const uint32_t* pix, uint32_t dim, uint32_t kind, uint32_t octant, int32_t part,
+                               const uint32_t* colors, uint32_t n_colors, const uint32_t* datas, uint32_t n_datas) {
+  Octree t;
+  t.color_palette.assign(colors, colors + n_colors);
+  t.data_palette.assign(datas, datas + n_datas);
+  BrickData b;
+  if (kind == 1) {
+    b.kind = B_SOLID;
+    b.solid = pix[0];
+  } else if (kind == 2) {
+    b.kind = B_PARTED;
+    b.parted.assign(pix, pix + (size_t)dim * dim * dim);
+  }
+  return guarded([&] {
+    const bool e = part < 0 ? t.is_empty_throughout(b, (uint8_t)octant, dim)
+                            : t.is_part_empty_throughout(b, (uint8_t)octant, (uint8_t)part, dim);
+    return e ? 1 : 0;
+  });
+}
+
 // NodeStack<T, SIZE> (raytracing_on_cpu.rs:20-82) with a runtime SIZE for the ring-stack tests
 struct StackHarness {
   std::vector<int32_t> data;

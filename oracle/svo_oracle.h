@@ -127,6 +127,8 @@ int orc_plane_line_intersection(const float plane_point[3], const float plane_no
 void orc_child_bounds(const float cube[4], uint32_t octant, float out[4]);
 void orc_dda_step(const float ray[6], float point[3], const float cube[4], float step_out[3]);
 uint64_t orc_flat_projection(uint64_t x, uint64_t y, uint64_t z, uint64_t size);
+int orc_brick_empty_throughout(const uint32_t* pix, uint32_t dim, uint32_t kind, uint32_t octant, int32_t part,
+                               const uint32_t* colors, uint32_t n_colors, const uint32_t* datas, uint32_t n_datas);
 
 /* Seeded synthetic workloads of the benchmark (oracle/workloads.cpp): the same op lists and rays as
    the product's svo_gen_scene / svo_gen_camera_rays / svo_gen_sphere_rays, so that the CPU baseline

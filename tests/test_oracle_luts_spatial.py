@@ -185,3 +185,52 @@ def test_node_stack(oracle_mod):
     for v in (5, 15, 25):
         s.push(v)
     assert [s.pop(), s.pop(), s.pop(), s.pop()] == [25, 15, 5, None]
+
+
+# ---- BrickData::is_empty_throughout / is_part_empty_throughout (src/octree/tests.rs:8-158) ----
+# The palettes of those tests: one colour (0, 0, 0, alpha 100) and one user datum 0; a voxel holds
+# colour index 0 and no datum (pix_visual(0)); the empty marker is u32::MAX.
+EMPTY_MARK = 0xFFFFFFFF
+PAL_C, PAL_D = [0x00000064], [0]
+OCTANT_OFFSET = [(0, 0, 0), (1, 0, 0), (0, 0, 1), (1, 0, 1), (0, 1, 0), (1, 1, 0), (0, 1, 1), (1, 1, 1)]
+
+
+def _brick(dim):  # every voxel pix_visual(0): colour index 0, no user datum
+    return [0xFFFF << 16] * dim ** 3
+
+
+def test_brick_octant_empty(oracle_mod):  # tests.rs:8-31
+    for o in range(8):
+        assert oracle_mod.brick_empty_throughout(0, [], 1, o, PAL_C, PAL_D)
+        assert not oracle_mod.brick_empty_throughout(2, _brick(1), 1, o, PAL_C, PAL_D)
+
+
+def test_brick_octant_empty_where_dim_is_2(oracle_mod):  # tests.rs:33-62
+    b = _brick(2)
+    assert not any(oracle_mod.brick_empty_throughout(2, b, 2, o, PAL_C, PAL_D) for o in range(8))
+    x, y, z = OCTANT_OFFSET[5]
+    b[oracle_mod.flat_projection(x, y, z, 2)] = EMPTY_MARK
+    assert oracle_mod.brick_empty_throughout(2, b, 2, 5, PAL_C, PAL_D)
+
+
+def test_brick_octant_empty_where_dim_is_4(oracle_mod):  # tests.rs:64-118
+    b = _brick(4)
+    assert not any(oracle_mod.brick_empty_throughout(2, b, 4, o, PAL_C, PAL_D) for o in range(8))
+    ox, oy, oz = (2 * v for v in OCTANT_OFFSET[5])
+    b[oracle_mod.flat_projection(ox, oy, oz, 4)] = EMPTY_MARK  # part of the octant: not yet empty
+    assert not oracle_mod.brick_empty_throughout(2, b, 4, 5, PAL_C, PAL_D)
+    for x in range(2):
+        for y in range(2):
+            for z in range(2):
+                b[oracle_mod.flat_projection(ox + x, oy + y, oz + z, 4)] = EMPTY_MARK
+    assert oracle_mod.brick_empty_throughout(2, b, 4, 5, PAL_C, PAL_D)
+
+
+def test_brick_part_of_octant_empty(oracle_mod):  # tests.rs:120-158
+    b = _brick(4)
+    assert not any(oracle_mod.brick_empty_throughout(2, b, 4, i, PAL_C, PAL_D, part=j)
+                   for i in range(8) for j in range(8))
+    ox, oy, oz = (2 * v for v in OCTANT_OFFSET[5])
+    b[oracle_mod.flat_projection(ox, oy, oz, 4)] = EMPTY_MARK
+    assert oracle_mod.brick_empty_throughout(2, b, 4, 5, PAL_C, PAL_D, part=0)
+    assert not oracle_mod.brick_empty_throughout(2, b, 4, 5, PAL_C, PAL_D, part=1)
