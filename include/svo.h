@@ -227,7 +227,8 @@ svo_status svo_cast_lod(svo_scene* scene, const svo_rays* rays, uint64_t n, cons
  * in chunks through a per-scene device workspace that grows on demand, copies overlapping the casts
  * (with pinned host memory); camera images given with their row length (svo_cast_host_rows) are
  * read and written in place where the device reads host memory through the CPU's page tables
- * (Grace), see svo_set_host_transfer. */
+ * (Grace), see svo_set_host_transfer: a large image (four claims or more per resident warp) is cast
+ * two 16 x 2 ray blocks per warp, each hit field written row by row in 32-ray pieces. */
 svo_status svo_cast_host(svo_scene* scene, const svo_rays* rays, uint64_t n, const svo_hits* hits, void* stream);
 /* The three casts above for rays laid out as rows of row_length rays (a camera image in raster
  * order, or several images one after the other): the work queue hands each warp 8 neighbouring rays
