@@ -118,3 +118,21 @@ def test_parity_helpers():
     assert bench.parity_failed({"comparisons": {"x": {"parity": m}}})
     assert not bench.parity_failed({"parity": bench.merge_parity([bench.compare_hits(same, ref)])})
     assert bench.parity_failed({"comparisons": {"served16": {"error": "RuntimeError: x"}}})
+
+
+def test_reported_figures_helpers():
+    """The arithmetic behind the reported figures: repeats to median and spread, the comparison with the
+    plain cast (a win counts as outside the spread only if the slowest repeat beats plain's fastest), and
+    the algorithmic bytes of a cast."""
+    n = 4_000_000
+    plain = bench.spread(n, [1.00, 1.02, 0.98])
+    assert plain["value"] == round(n / 1.00e-3 / 1e6, 3) and plain["ms_per_step"] == 1.0 and plain["repeats"] == 3
+    assert plain["min"] == round(n / 1.02e-3 / 1e6, 3) and plain["max"] == round(n / 0.98e-3 / 1e6, 3)
+    close = bench.spread(n, [0.97, 0.99, 0.96])  # faster median, but its slowest repeat is inside plain's spread
+    v = bench.versus(close, plain)
+    assert v["beats_plain"] and not v["beats_plain_outside_spread"] and v["median_ratio"] > 1
+    clear = bench.spread(n, [0.90, 0.91, 0.89])
+    assert bench.versus(clear, plain)["beats_plain_outside_spread"]
+    assert not bench.versus(bench.spread(n, [1.1, 1.1, 1.1]), plain)["beats_plain"]
+    # 12 B per performed visit, 4 B per child read and per voxel tested, 8 B per hit
+    assert bench.alg_bytes_of(10, 3, 2, 1) == 120 + 12 + 8 + 8
